@@ -1,0 +1,93 @@
+"""ctypes binding of libbfe_gb300.so (the C ABI declared in include/bfe_gb300.h).
+
+The library must exist: there is no CPU fallback. ``load()`` raises if the
+shared object is missing or does not export every declared entry point.
+"""
+import ctypes
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libbfe_gb300.so")
+
+BFE_OK = 0
+BFE_ERR_ARG = 1
+BFE_ERR_OOM = 2
+BFE_ERR_CUDA = 3
+BFE_ERR_NUMERIC = 4
+BFE_ERR_UNSUPPORTED = 5
+BFE_ERR_NO_DEVICE = 6
+STATUS_NAMES = {0: "BFE_OK", 1: "BFE_ERR_ARG", 2: "BFE_ERR_OOM", 3: "BFE_ERR_CUDA",
+                4: "BFE_ERR_NUMERIC", 5: "BFE_ERR_UNSUPPORTED", 6: "BFE_ERR_NO_DEVICE"}
+
+BFE_CSR = 0
+BFE_CSC = 1
+BFE_MODE_VEL_CURRENT = 0
+BFE_MODE_VEL_LAST_HALF = 1
+BFE_PREC_DOUBLE = 0
+BFE_PREC_SINGLE = 1
+
+I64 = ctypes.c_int64
+I32 = ctypes.c_int32
+PD = ctypes.POINTER(ctypes.c_double)
+PI64 = ctypes.POINTER(ctypes.c_int64)
+PI32 = ctypes.POINTER(ctypes.c_int32)
+VP = ctypes.c_void_p
+
+
+class BfeSparse(ctypes.Structure):
+    _fields_ = [("n_rows", I64), ("n_cols", I64), ("nnz", I64), ("format", I32),
+                ("ptr", PI64), ("idx", PI64), ("val", PD)]
+
+
+SIGNATURES = {
+    "bfe_plan_create": (I32, [ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
+                              ctypes.POINTER(BfeSparse), ctypes.c_double, I32, I32,
+                              PI64, PI32, ctypes.POINTER(VP)]),
+    "bfe_plan_destroy": (I32, [VP]),
+    "bfe_plan_ndof": (I32, [VP, PI64]),
+    "bfe_run": (I32, [VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, I32, PD, PD, PD]),
+    "bfe_run_batched": (I32, [VP, I64, I64, PD, I64, PI64, I64, PD, I64, PI64, PD]),
+    "bfe_run_device": (I32, [VP, I64, I64, I64, I64, PI64, PI64, PI64, PD, I64, VP,
+                             I64, PI64, VP, VP]),
+    "bfe_last_error": (ctypes.c_char_p, []),
+    "bfe_version": (I32, [PI32, PI32, PI32]),
+}
+
+_lib = None
+
+
+class BfeError(RuntimeError):
+    """A non-zero status returned across the C ABI."""
+
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+
+
+def load():
+    """Load the native library (once). Raises if it is missing or incomplete."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libbfe_gb300.so not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)          # AttributeError if not exported
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status):
+    if status != BFE_OK:
+        msg = load().bfe_last_error()
+        raise BfeError(status, msg.decode() if msg else "")
+
+
+def ptr(a, ctype):
+    """ctypes pointer to a contiguous numpy array (or NULL for None)."""
+    if a is None:
+        return ctypes.cast(None, ctypes.POINTER(ctype))
+    return a.ctypes.data_as(ctypes.POINTER(ctype))

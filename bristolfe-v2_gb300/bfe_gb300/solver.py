@@ -1,0 +1,233 @@
+"""Host-side mirror of the reference's time-marching call, backed by the C ABI.
+
+``fn_explicit_dynamic_solver_gb300`` takes the arguments of
+``fn_explicit_dynamic_solver_v6`` (code/internal/fn_explicit_dynamic_solver_v6.m:1-5)
+with the same meaning - including 1-based global indices and MATLAB-shaped
+arrays - and returns the same four outputs. All arithmetic runs in the native
+library on the GPU; there is no CPU path here.
+"""
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from ._lib import BfeError, check, ptr
+
+VEL_LAST_HALF = "vel at last half time step"     # v6.m:131
+VEL_CURRENT = "vel at curent time step"          # v6.m:135 (sic)
+DISP_FIELD_TYPES = ("mean(u1)", "mean(u2)", "mean(u3)", "curl(u)", "div(u)", "raw(u)")  # v6.m:64-69
+
+_MODES = {VEL_CURRENT: _lib.BFE_MODE_VEL_CURRENT, VEL_LAST_HALF: _lib.BFE_MODE_VEL_LAST_HALF}
+
+
+class SolverError(RuntimeError):
+    """Raised where the reference solver raises (or fails) for the same input."""
+
+
+def _mode_code(solver_mode):
+    try:
+        return _MODES[solver_mode]
+    except KeyError:
+        # v6.m:130-139 leaves A, B, D undefined for any other string
+        raise SolverError("unknown solver_mode %r (accepted: %r, %r)"
+                          % (solver_mode, VEL_CURRENT, VEL_LAST_HALF)) from None
+
+
+def _precision_code(solver_precision):
+    s = str(solver_precision).lower()
+    if s == "single":
+        return _lib.BFE_PREC_SINGLE
+    if s == "double":
+        return _lib.BFE_PREC_DOUBLE
+    raise SolverError("solver_precision must be 'double' or 'single', got %r" % (solver_precision,))
+
+
+def _csr_view(A, name):
+    A = sp.csr_matrix(A)
+    A.sum_duplicates()
+    ptr_ = np.ascontiguousarray(A.indptr, dtype=np.int64)
+    idx = np.ascontiguousarray(A.indices, dtype=np.int64)
+    val = np.ascontiguousarray(A.data, dtype=np.float64)
+    s = _lib.BfeSparse(A.shape[0], A.shape[1], val.size, _lib.BFE_CSR,
+                       ptr(ptr_, ctypes.c_int64), ptr(idx, ctypes.c_int64), ptr(val, ctypes.c_double))
+    return s, (ptr_, idx, val)
+
+
+def dof_maps_from_lookup(gl_lookup, n):
+    """(dof_node, dof_type) per global DOF from a reference gl_lookup matrix
+    (rows = nodes, cols = DOF numbers, entries = 1-based global indices)."""
+    gl = np.asarray(gl_lookup, dtype=np.int64)
+    node = np.full(n, -1, np.int64)
+    typ = np.zeros(n, np.int32)
+    a, d = np.nonzero(gl > 0)
+    g = gl[a, d] - 1
+    if g.size and (g.max() >= n):
+        raise SolverError("gl_lookup refers to DOFs beyond the matrix size")
+    node[g] = a
+    typ[g] = d + 1
+    if np.any(node < 0):
+        raise SolverError("gl_lookup does not cover every DOF")
+    return node, typ
+
+
+class Plan:
+    """Device-resident time-stepping operator (one bfe_plan)."""
+
+    def __init__(self, K, C, M, dt, solver_mode=VEL_CURRENT, solver_precision="double",
+                 gl_lookup=None):
+        lib = _lib.load()
+        self._lib = lib
+        self.mode = _mode_code(solver_mode)
+        self.precision = _precision_code(solver_precision)
+        self.dt = float(dt)
+        n = K.shape[0]
+        Ks, keepK = _csr_view(K, "K")
+        Cs, keepC = _csr_view(C, "C")
+        Ms, keepM = _csr_view(M, "M")
+        node = typ = None
+        if gl_lookup is not None:
+            node, typ = dof_maps_from_lookup(gl_lookup, n)
+        handle = ctypes.c_void_p()
+        st = lib.bfe_plan_create(ctypes.byref(Ks), ctypes.byref(Cs), ctypes.byref(Ms), self.dt,
+                                 self.mode, self.precision, ptr(node, ctypes.c_int64),
+                                 ptr(typ, ctypes.c_int32), ctypes.byref(handle))
+        check(st)
+        self._h = handle
+        nn = ctypes.c_int64()
+        check(lib.bfe_plan_ndof(self._h, ctypes.byref(nn)))
+        self.n = nn.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.bfe_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def run(self, time, forcing_indices, forcing_functions, history_indices,
+            field_output_every_n_frames=np.inf, field_is_vel=True):
+        """One load step (1-based indices). Returns (hist q x n_t, fld or None, fld_time or None)."""
+        time = np.ascontiguousarray(np.asarray(time, float).ravel())
+        nt = time.size
+        fi = np.ascontiguousarray(np.asarray(forcing_indices, np.int64).ravel() - 1) \
+            if forcing_indices is not None else np.zeros(0, np.int64)
+        p = fi.size
+        F = None
+        rows = 0
+        if p:
+            F = np.atleast_2d(np.asarray(forcing_functions, float))
+            if F.shape[1] < nt:
+                raise SolverError("forcing_functions has fewer columns than time samples")
+            F = np.asfortranarray(F[:, :nt])
+            rows = F.shape[0]
+        hi = np.ascontiguousarray(np.asarray(history_indices, np.int64).ravel() - 1) \
+            if history_indices is not None else np.zeros(0, np.int64)
+        q = hi.size
+        hist = np.zeros((q, nt), order="F")
+        every = 0 if np.isinf(field_output_every_n_frames) else int(field_output_every_n_frames)
+        fld = fld_t = None
+        if every > 0:
+            nf = (nt + every - 1) // every
+            fld = np.zeros((self.n, nf), order="F")
+            fld_t = np.zeros(nf)
+        st = self._lib.bfe_run(self._h, nt, ptr(time, ctypes.c_double), p, ptr(fi, ctypes.c_int64),
+                               rows, ptr(F, ctypes.c_double), q, ptr(hi, ctypes.c_int64),
+                               every, int(bool(field_is_vel)), ptr(hist, ctypes.c_double),
+                               ptr(fld, ctypes.c_double), ptr(fld_t, ctypes.c_double))
+        check(st)
+        return hist, fld, fld_t
+
+    def run_batched(self, time, forcing_indices_per_source, forcing_functions, history_indices):
+        """R load steps sharing this operator as one multi-RHS march.
+
+        forcing_indices_per_source: list of R 1-based index arrays (ragged ok);
+        forcing_functions: (rows, n_t) shared by all sources or (rows, n_t, R),
+        rows = 1 (broadcast) or the (common) number of forced DOFs.
+        Returns hist of shape (q, n_t, R)."""
+        time = np.ascontiguousarray(np.asarray(time, float).ravel())
+        nt = time.size
+        R = len(forcing_indices_per_source)
+        p = max((len(np.ravel(x)) for x in forcing_indices_per_source), default=0)
+        fi = np.full((p, R), -1, np.int64, order="F")
+        for r, x in enumerate(forcing_indices_per_source):
+            x = np.asarray(x, np.int64).ravel() - 1
+            fi[: x.size, r] = x
+        F = np.asarray(forcing_functions, float)
+        if F.ndim == 1:
+            F = F[None, :]
+        if F.ndim == 2:
+            F = np.repeat(F[:, :nt, None], R, axis=2)
+        F = np.asfortranarray(F[:, :nt, :])
+        rows = F.shape[0]
+        hi = np.ascontiguousarray(np.asarray(history_indices, np.int64).ravel() - 1)
+        q = hi.size
+        hist = np.zeros((q, nt, R), order="F")
+        st = self._lib.bfe_run_batched(self._h, R, nt, ptr(time, ctypes.c_double), p,
+                                       ptr(fi, ctypes.c_int64), rows, ptr(F, ctypes.c_double),
+                                       q, ptr(hi, ctypes.c_int64), ptr(hist, ctypes.c_double))
+        check(st)
+        return hist
+
+    def run_device(self, R, n_t, ti_start, frc_dof, frc_rhs, frc_sig, frc_w, d_sig, hist_idx,
+                   d_hist, stream=0):
+        """Device-resident march: d_sig / d_hist are torch CUDA tensors (FP64).
+
+        frc_* are 0-based host arrays; d_hist must be zeroed, shape (R, n_t, q)
+        in C order == q x n_t x R column-major."""
+        frc_dof = np.ascontiguousarray(frc_dof, np.int64)
+        frc_rhs = np.ascontiguousarray(frc_rhs, np.int64)
+        frc_sig = np.ascontiguousarray(frc_sig, np.int64)
+        frc_w = None if frc_w is None else np.ascontiguousarray(frc_w, np.float64)
+        hist_idx = np.ascontiguousarray(hist_idx, np.int64)
+        st = self._lib.bfe_run_device(
+            self._h, int(R), int(n_t), int(ti_start), frc_dof.size, ptr(frc_dof, ctypes.c_int64),
+            ptr(frc_rhs, ctypes.c_int64), ptr(frc_sig, ctypes.c_int64),
+            ptr(frc_w, ctypes.c_double), int(d_sig.shape[-1]) if d_sig is not None else 0,
+            ctypes.c_void_p(d_sig.data_ptr() if d_sig is not None else 0),
+            hist_idx.size, ptr(hist_idx, ctypes.c_int64),
+            ctypes.c_void_p(d_hist.data_ptr() if d_hist is not None else 0),
+            ctypes.c_void_p(int(stream)))
+        check(st)
+
+
+def fn_explicit_dynamic_solver_gb300(K, C, M, time, forcing_indices, forcing_functions,
+                                     disp_indices, disp_functions, history_indices,
+                                     field_output_every_n_frames, use_gpu_if_present=1,
+                                     field_output_type="KE", solver_mode=VEL_CURRENT,
+                                     solver_precision="double", gl_lookup=None):
+    """Drop-in for fn_explicit_dynamic_solver_v6 (same 14 arguments, 1-based
+    indices). Returns (history_output, field_output, force_output,
+    field_output_time); force_output is always None because prescribed
+    displacements are rejected, as in the reference's v6 path (v6.m:191).
+
+    ``gl_lookup`` (optional, the builder's node/DOF lookup) enables the
+    translation-invariant FP32 stiffness product."""
+    if K.shape[0] != K.shape[1]:
+        raise SolverError("K must be square matrix")
+    if C.shape[0] != C.shape[1]:
+        raise SolverError("C must be square matrix")
+    if M.shape[0] != M.shape[1]:
+        raise SolverError("M must be square matrix")
+    if disp_indices is not None and len(np.ravel(disp_indices)):
+        raise SolverError("prescribed displacements are not supported by the v6 path "
+                          "(the reference reads an undefined u_previous, v6.m:191)")
+    time = np.asarray(time, float).ravel()
+    dt = time[1] - time[0]
+    is_vel = field_output_type not in DISP_FIELD_TYPES
+    with Plan(K, C, M, dt, solver_mode, solver_precision, gl_lookup) as plan:
+        hist, fld, fld_t = plan.run(time, forcing_indices, forcing_functions, history_indices,
+                                    field_output_every_n_frames, is_vel)
+    if history_indices is None or len(np.ravel(history_indices)) == 0:
+        hist = None
+    return hist, fld, None, fld_t

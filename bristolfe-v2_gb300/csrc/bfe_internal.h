@@ -1,0 +1,81 @@
+// Internal declarations shared by the host plan code and the CUDA kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bfe {
+
+// Sliced-ELL slice height: one warp of rows per slice.
+constexpr int kSlice = 32;
+
+// Packed entry word of the FP32 operator: bits 0-27 column, bits 28-30 the
+// slot (position inside the row's node block) of the DOF whose value is
+// subtracted (difference form), bit 31 set = direct term (no subtraction).
+constexpr uint32_t kColMask = 0x0FFFFFFFu;
+constexpr uint32_t kDirect = 0x80000000u;
+constexpr int kSlotShift = 28;
+constexpr uint32_t kSlotMask = 0x7u;
+
+// Per-row info word: bits 0-27 node-block base (first DOF of the row's node
+// block), bit 28 forced, bit 29 monitored, bit 30 interface row.
+constexpr uint32_t kBaseMask = 0x0FFFFFFFu;
+constexpr uint32_t kRowForced = 1u << 28;
+constexpr uint32_t kRowMonitored = 1u << 29;
+constexpr uint32_t kRowInterface = 1u << 30;
+
+// Maximum DOFs addressable by the packed words.
+constexpr int64_t kMaxDof = (int64_t)kColMask;
+
+// Device view of everything one time step needs (passed by value).
+struct StepArgs {
+  int32_t n;            // rows (DOFs)
+  int32_t R;            // right-hand sides (state is [n][R], RHS-contiguous)
+  int32_t n_slices;
+  const int32_t* slice_ptr;   // entry offset of each slice (n_slices + 1)
+  const uint32_t* col;        // packed entries, column-major inside a slice
+  const void* val;            // double (FP64 plan) or float (FP32 plan)
+  const void* rowc;           // FP64: coefficient of u_{n-1}; FP32: q_i
+  const uint32_t* rowinfo;    // per-row info word (this run's flags)
+  // forcing entries sorted by row: row, rhs, signal row, coefficient
+  int32_t n_frc;
+  const int32_t* frc_row;
+  const int32_t* frc_rhs;
+  const int32_t* frc_sig;
+  const void* frc_coef;       // double / float
+  const void* sig;            // [n_t][n_sig] time-major, double / float
+  int32_t n_sig;
+  // monitors sorted by row: row, history slot
+  int32_t n_mon;
+  const int32_t* mon_row;
+  const int32_t* mon_slot;
+  int32_t q;                  // history slots per RHS
+  int64_t n_t;
+  double* hist;               // hist[slot + q * (ti + n_t * r)]
+  // interface rows (sorted) and their correction operator Z (CSR over the
+  // compact interface numbering)
+  int32_t n_int;
+  const int32_t* int_row;
+  const int32_t* z_ptr;
+  const int32_t* z_col;
+  const void* z_val;
+  int32_t int_base_prev;      // 1: u_new = u_{n-1} + Z v, 0: u_new += Z v
+  void* v_int;                // scratch [n_int][R]
+  // states: u_n (read), u_{n-1} (read), u_{n+1} (write)
+  const void* u_n;
+  const void* u_prev;
+  void* u_new;
+  int64_t ti;                 // 0-based time index of the computed state
+};
+
+// Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.
+cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
+cudaError_t launch_step_batched(const StepArgs& a, int precision, int max_slice_entries,
+                                cudaStream_t s);                                      // any R
+size_t batched_smem_bytes(int precision, int max_slice_entries);
+cudaError_t set_batched_smem_limit(int precision, size_t smem);
+cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);
+cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t frame,
+                         int field_is_vel, double dt, cudaStream_t s);
+cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
+
+}  // namespace bfe

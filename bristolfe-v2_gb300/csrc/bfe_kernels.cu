@@ -1,0 +1,334 @@
+// Time-step kernels of the GB300 explicit solver (sm_103a).
+//
+// One time step of fn_explicit_dynamic_solver_v6.m:180-218 is
+//     u_{n+1} = A f + B u_n + D u_{n-1}
+// (v6.m:185). The operator is stored as a sliced ELL matrix (slices of 32
+// rows, entries column-major inside a slice) so that a warp of consecutive
+// rows reads its matrix entries with coalesced loads.
+//
+//  * FP64 plans keep the reference's arithmetic: B (with its diagonal) in
+//    the slice entries, the diagonal D in rowc, forcing coefficients of the
+//    diagonal A in the forcing list.
+//  * FP32 plans use the equivalent increment form
+//        u_{n+1} = u_n + q (u_n - u_{n-1}) - Lp u_n + forcing
+//    where Lp = P^-1 dt^2 M^-1 K and q = P^-1 (1 - dt/2 M^-1 C) for the
+//    diagonal part of P. The stiffness product is evaluated in the
+//    difference form sum_j Lp_ij (u_j - u_{node(i), dof(j)}), which is exact
+//    for rigid translations whatever the FP32 rounding of Lp, and the update
+//    is evaluated with an error-free two-sum of (u_n - u_{n-1}).
+//  * Interface rows (fluid-solid coupling in C) get the exact implicit part
+//    in a second small kernel: v = (u_hat - u_{n-1}) or (u_n - u_{n-1})
+//    is staged per interface row, then u_new = base + Z v.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "bfe_internal.h"
+
+namespace bfe {
+
+template <typename T> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
+__device__ __forceinline__ int lower_bound_i32(const int32_t* a, int n, int key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(a + mid) < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Sum of coef * signal over the forcing entries of row i for right-hand side r.
+template <typename T>
+__device__ __forceinline__ T forcing_sum(const StepArgs& a, int i, int r) {
+  const T* coef = static_cast<const T*>(a.frc_coef);
+  const T* sig = static_cast<const T*>(a.sig) + (size_t)a.ti * a.n_sig;
+  T f = T(0);
+  for (int e = lower_bound_i32(a.frc_row, a.n_frc, i); e < a.n_frc && __ldg(a.frc_row + e) == i; ++e) {
+    if (__ldg(a.frc_rhs + e) == r) f += __ldg(coef + e) * __ldg(sig + __ldg(a.frc_sig + e));
+  }
+  return f;
+}
+
+__device__ __forceinline__ void write_history(const StepArgs& a, int i, int r, double v) {
+  for (int k = lower_bound_i32(a.mon_row, a.n_mon, i); k < a.n_mon && __ldg(a.mon_row + k) == i; ++k) {
+    int slot = __ldg(a.mon_slot + k);
+    a.hist[(size_t)slot + (size_t)a.q * ((size_t)a.ti + (size_t)a.n_t * r)] = v;
+  }
+}
+
+// Error-free transformation: s + e == a + b exactly (Knuth two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// ---------------------------------------------------------------------------
+// FP64, one right-hand side: one thread per row.
+__global__ void __launch_bounds__(256) step_f64_r1(StepArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int s = i >> 5, lane = i & 31;
+  const int off = __ldg(a.slice_ptr + s);
+  const int w = (__ldg(a.slice_ptr + s + 1) - off) >> 5;
+  const uint32_t* col = a.col + off + lane;
+  const double* val = static_cast<const double*>(a.val) + off + lane;
+  const double* un = static_cast<const double*>(a.u_n);
+  double acc = 0.0;
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) {
+    acc = fma(__ldg(val + 32 * k), __ldg(un + __ldg(col + 32 * k)), acc);
+  }
+  const uint32_t info = __ldg(a.rowinfo + i);
+  const double up = static_cast<const double*>(a.u_prev)[i];
+  double r = acc + __ldg(static_cast<const double*>(a.rowc) + i) * up;
+  if (info & kRowForced) r += forcing_sum<double>(a, i, 0);
+  static_cast<double*>(a.u_new)[i] = r;
+  if (info & kRowInterface) {
+    const int t = lower_bound_i32(a.int_row, a.n_int, i);
+    static_cast<double*>(a.v_int)[t] = a.int_base_prev ? (r - up) : (un[i] - up);
+  } else if (info & kRowMonitored) {
+    write_history(a, i, 0, r);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32, one right-hand side: one thread per row, difference form.
+__global__ void __launch_bounds__(256) step_f32_r1(StepArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int s = i >> 5, lane = i & 31;
+  const int off = __ldg(a.slice_ptr + s);
+  const int w = (__ldg(a.slice_ptr + s + 1) - off) >> 5;
+  const uint32_t* col = a.col + off + lane;
+  const float* val = static_cast<const float*>(a.val) + off + lane;
+  const float* un = static_cast<const float*>(a.u_n);
+  const uint32_t info = __ldg(a.rowinfo + i);
+  const uint32_t base = info & kBaseMask;
+  float acc = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) {
+    const uint32_t e = __ldg(col + 32 * k);
+    const float uj = __ldg(un + (e & kColMask));
+    const float ur = (e & kDirect) ? 0.f : __ldg(un + base + ((e >> kSlotShift) & kSlotMask));
+    acc = fmaf(__ldg(val + 32 * k), uj - ur, acc);
+  }
+  const float ui = un[i];
+  const float up = static_cast<const float*>(a.u_prev)[i];
+  const float q = __ldg(static_cast<const float*>(a.rowc) + i);
+  float d, err;
+  two_sum(ui, -up, d, err);
+  float inc = fmaf(q, d, -acc);
+  if (info & kRowForced) inc += forcing_sum<float>(a, i, 0);
+  inc = fmaf(q, err, inc);
+  const float r = ui + inc;
+  static_cast<float*>(a.u_new)[i] = r;
+  if (info & kRowInterface) {
+    const int t = lower_bound_i32(a.int_row, a.n_int, i);
+    static_cast<float*>(a.v_int)[t] = a.int_base_prev ? (d + err + inc) : (d + err);
+  } else if (info & kRowMonitored) {
+    write_history(a, i, 0, (double)r);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched (R right-hand sides, state [n][R]). One CTA per slice of 32 rows:
+// the slice's matrix entries are staged in shared memory with coalesced
+// loads, then each warp takes rows of the slice and its lanes take the
+// right-hand sides, so every gathered state row is one contiguous R-vector.
+template <typename T, int VEC>
+__global__ void __launch_bounds__(256) step_batched(StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int s = blockIdx.x;
+  const int off = __ldg(a.slice_ptr + s);
+  const int ne = __ldg(a.slice_ptr + s + 1) - off;
+  const int w = ne >> 5;
+  uint32_t* scol = reinterpret_cast<uint32_t*>(smem_raw);
+  T* sval = reinterpret_cast<T*>(smem_raw + ((ne * sizeof(uint32_t) + 15) & ~size_t(15)));
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    scol[e] = __ldg(a.col + off + e);
+    sval[e] = __ldg(static_cast<const T*>(a.val) + off + e);
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int R = a.R;
+  const T* un = static_cast<const T*>(a.u_n);
+  const T* upv = static_cast<const T*>(a.u_prev);
+  T* unew = static_cast<T*>(a.u_new);
+  for (int rr = warp; rr < kSlice; rr += nwarps) {
+    const int i = s * kSlice + rr;
+    if (i >= a.n) break;
+    const uint32_t info = __ldg(a.rowinfo + i);
+    const uint32_t base = info & kBaseMask;
+    const T rc = __ldg(static_cast<const T*>(a.rowc) + i);
+    for (int c0 = lane * VEC; c0 < R; c0 += 32 * VEC) {
+      T acc[VEC];
+#pragma unroll
+      for (int v = 0; v < VEC; ++v) acc[v] = T(0);
+#pragma unroll 2
+      for (int k = 0; k < w; ++k) {
+        const uint32_t e = scol[k * kSlice + rr];
+        const T lv = sval[k * kSlice + rr];
+        const size_t j = (size_t)(e & kColMask);
+        if constexpr (sizeof(T) == 4) {
+          const size_t jr = (size_t)base + ((e >> kSlotShift) & kSlotMask);
+          const bool direct = (e & kDirect) != 0;
+          if constexpr (VEC == 2) {
+            const float2 uj = __ldg(reinterpret_cast<const float2*>(un + j * R + c0));
+            float2 ur = make_float2(0.f, 0.f);
+            if (!direct) ur = __ldg(reinterpret_cast<const float2*>(un + jr * R + c0));
+            acc[0] = fmaf(lv, uj.x - ur.x, acc[0]);
+            acc[1] = fmaf(lv, uj.y - ur.y, acc[1]);
+          } else {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+              const float uj = __ldg(un + j * R + c0 + v);
+              const float ur = direct ? 0.f : __ldg(un + jr * R + c0 + v);
+              acc[v] = fmaf(lv, uj - ur, acc[v]);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int v = 0; v < VEC; ++v) acc[v] = fma(lv, __ldg(un + j * R + c0 + v), acc[v]);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < VEC; ++v) {
+        const int c = c0 + v;
+        const size_t o = (size_t)i * R + c;
+        const T ui = un[o];
+        const T up = upv[o];
+        T r, vint;
+        if constexpr (sizeof(T) == 4) {
+          float d, err;
+          two_sum(ui, -up, d, err);
+          float inc = fmaf(rc, d, -acc[v]);
+          if (info & kRowForced) inc += forcing_sum<float>(a, i, c);
+          inc = fmaf(rc, err, inc);
+          r = ui + inc;
+          vint = a.int_base_prev ? (d + err + inc) : (d + err);
+        } else {
+          r = acc[v] + rc * up;
+          if (info & kRowForced) r += forcing_sum<double>(a, i, c);
+          vint = a.int_base_prev ? (r - up) : (ui - up);
+        }
+        unew[o] = r;
+        if (info & kRowInterface) {
+          const int t = lower_bound_i32(a.int_row, a.n_int, i);
+          static_cast<T*>(a.v_int)[(size_t)t * R + c] = vint;
+        } else if (info & kRowMonitored) {
+          write_history(a, i, c, (double)r);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
+// per (interface row, right-hand side).
+template <typename T>
+__global__ void __launch_bounds__(256) interface_fixup(StepArgs a) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int R = a.R;
+  if (g >= (int64_t)a.n_int * R) return;
+  const int t = (int)(g / R), c = (int)(g % R);
+  const int row = __ldg(a.int_row + t);
+  const T* z = static_cast<const T*>(a.z_val);
+  const T* v = static_cast<const T*>(a.v_int);
+  T acc = T(0);
+  for (int e = __ldg(a.z_ptr + t); e < __ldg(a.z_ptr + t + 1); ++e) {
+    acc += __ldg(z + e) * v[(size_t)__ldg(a.z_col + e) * R + c];
+  }
+  const size_t o = (size_t)row * R + c;
+  T* unew = static_cast<T*>(a.u_new);
+  const T base = a.int_base_prev ? static_cast<const T*>(a.u_prev)[o] : unew[o];
+  const T r = base + acc;
+  unew[o] = r;
+  if (__ldg(a.rowinfo + row) & kRowMonitored) write_history(a, row, c, (double)r);
+}
+
+// Field frame: fld[i + n * frame] = (u_new - u_n) / dt or u_new (R = 1).
+template <typename T>
+__global__ void frame_kernel(StepArgs a, double* fld, int64_t frame, int is_vel, double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double un = (double)static_cast<const T*>(a.u_new)[i];
+  const double uo = (double)static_cast<const T*>(a.u_n)[i];
+  fld[(size_t)i + (size_t)a.n * frame] = is_vel ? (un - uo) / dt : un;
+}
+
+__global__ void cast_kernel(const double* in, float* out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
+// ---------------------------------------------------------------------------
+cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t st) {
+  const int threads = 256;
+  const int blocks = (a.n + threads - 1) / threads;
+  if (precision == 0) step_f64_r1<<<blocks, threads, 0, st>>>(a);
+  else step_f32_r1<<<blocks, threads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+size_t batched_smem_bytes(int precision, int max_slice_entries) {
+  const size_t elem = precision == 0 ? sizeof(double) : sizeof(float);
+  return ((size_t(max_slice_entries) * 4 + 15) & ~size_t(15)) + size_t(max_slice_entries) * elem;
+}
+
+cudaError_t launch_step_batched(const StepArgs& a, int precision, int max_slice_entries,
+                                cudaStream_t st) {
+  const int threads = 256;
+  const size_t smem = batched_smem_bytes(precision, max_slice_entries);
+  if (precision == 0) {
+    step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
+  } else {
+    if (a.R % 64 == 0) step_batched<float, 2><<<a.n_slices, threads, smem, st>>>(a);
+    else step_batched<float, 1><<<a.n_slices, threads, smem, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t set_batched_smem_limit(int precision, size_t smem) {
+  cudaError_t e;
+  if (precision == 0) {
+    e = cudaFuncSetAttribute(step_batched<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  } else {
+    e = cudaFuncSetAttribute(step_batched<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(step_batched<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  return e;
+}
+
+cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t st) {
+  if (a.n_int == 0) return cudaSuccess;
+  const int threads = 256;
+  const int64_t total = (int64_t)a.n_int * a.R;
+  const int blocks = (int)((total + threads - 1) / threads);
+  if (precision == 0) interface_fixup<double><<<blocks, threads, 0, st>>>(a);
+  else interface_fixup<float><<<blocks, threads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t frame,
+                         int field_is_vel, double dt, cudaStream_t st) {
+  const int threads = 256;
+  const int blocks = (a.n + threads - 1) / threads;
+  if (precision == 0) frame_kernel<double><<<blocks, threads, 0, st>>>(a, fld, frame, field_is_vel, dt);
+  else frame_kernel<float><<<blocks, threads, 0, st>>>(a, fld, frame, field_is_vel, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int threads = 256;
+  cast_kernel<<<(int)((n + threads - 1) / threads), threads, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+}  // namespace bfe

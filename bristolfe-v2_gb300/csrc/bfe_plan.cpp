@@ -1,0 +1,873 @@
+// Host side of the C ABI: operator formation (FP64), device layout, and the
+// time loop of one load step. Kernels live in bfe_kernels.cu.
+//
+// Reference being replaced: code/internal/fn_explicit_dynamic_solver_v6.m
+// (operator formation :122-159, time loop :161-218) as called from
+// code/fn_BristolFE_v2.m:120-122.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "bfe_internal.h"
+#include "../../include/bfe_gb300.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                \
+  do {                                                                                \
+    cudaError_t e_ = (expr);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(e_ == cudaErrorMemoryAllocation ? BFE_ERR_OOM : BFE_ERR_CUDA,       \
+                  "%s failed: %s", #expr, cudaGetErrorString(e_));                    \
+  } while (0)
+
+// Row-compressed FP64 matrix used during plan construction.
+struct Csr {
+  int64_t n = 0, m = 0;
+  std::vector<int64_t> ptr, idx;
+  std::vector<double> val;
+};
+
+// Copy a bfe_sparse view into sorted, duplicate-summed CSR.
+int to_csr(const bfe_sparse* A, const char* name, Csr& out) {
+  if (!A) return fail(BFE_ERR_ARG, "%s is NULL", name);
+  if (A->n_rows < 0 || A->n_cols < 0 || A->nnz < 0) return fail(BFE_ERR_ARG, "%s has negative sizes", name);
+  if (A->nnz > 0 && (!A->ptr || !A->idx || !A->val)) return fail(BFE_ERR_ARG, "%s has NULL arrays", name);
+  if (A->format != BFE_CSR && A->format != BFE_CSC) return fail(BFE_ERR_ARG, "%s: unknown format %d", name, A->format);
+  const bool csc = A->format == BFE_CSC;
+  const int64_t nmaj = csc ? A->n_cols : A->n_rows;
+  const int64_t nmin = csc ? A->n_rows : A->n_cols;
+  if (A->ptr && (A->ptr[0] != 0 || A->ptr[nmaj] != A->nnz)) return fail(BFE_ERR_ARG, "%s: bad pointer array", name);
+  std::vector<int64_t> rows, cols;
+  rows.reserve(A->nnz);
+  cols.reserve(A->nnz);
+  for (int64_t a = 0; a < nmaj; ++a) {
+    if (A->ptr[a + 1] < A->ptr[a]) return fail(BFE_ERR_ARG, "%s: pointer array not monotone", name);
+    for (int64_t e = A->ptr[a]; e < A->ptr[a + 1]; ++e) {
+      const int64_t b = A->idx[e];
+      if (b < 0 || b >= nmin) return fail(BFE_ERR_ARG, "%s: index %lld out of range", name, (long long)b);
+      if (!std::isfinite(A->val[e])) return fail(BFE_ERR_NUMERIC, "%s has a non-finite value", name);
+      rows.push_back(csc ? b : a);
+      cols.push_back(csc ? a : b);
+    }
+  }
+  out.n = A->n_rows;
+  out.m = A->n_cols;
+  out.ptr.assign(out.n + 1, 0);
+  for (int64_t r : rows) out.ptr[r + 1]++;
+  for (int64_t i = 0; i < out.n; ++i) out.ptr[i + 1] += out.ptr[i];
+  std::vector<int64_t> pos(out.ptr.begin(), out.ptr.end() - 1);
+  std::vector<int64_t> ci(rows.size());
+  std::vector<double> cv(rows.size());
+  for (size_t e = 0; e < rows.size(); ++e) {
+    const int64_t p = pos[rows[e]]++;
+    ci[p] = cols[e];
+    cv[p] = A->val[e];
+  }
+  // sort each row, sum duplicates, drop exact zeros (MATLAB keeps non-zeros)
+  std::vector<int64_t> nptr(out.n + 1, 0);
+  out.idx.clear();
+  out.val.clear();
+  std::vector<std::pair<int64_t, double>> tmp;
+  for (int64_t i = 0; i < out.n; ++i) {
+    tmp.clear();
+    for (int64_t e = out.ptr[i]; e < out.ptr[i + 1]; ++e) tmp.emplace_back(ci[e], cv[e]);
+    std::sort(tmp.begin(), tmp.end(), [](auto& x, auto& y) { return x.first < y.first; });
+    size_t k = 0;
+    while (k < tmp.size()) {
+      int64_t c = tmp[k].first;
+      double s = 0;
+      while (k < tmp.size() && tmp[k].first == c) s += tmp[k++].second;
+      if (s != 0.0) {
+        out.idx.push_back(c);
+        out.val.push_back(s);
+      }
+    }
+    nptr[i + 1] = (int64_t)out.idx.size();
+  }
+  out.ptr.swap(nptr);
+  return BFE_OK;
+}
+
+// Sparse product with dropping: C = A * B (both over the same index space).
+Csr spgemm(const Csr& A, const Csr& B, double rel_drop) {
+  Csr C;
+  C.n = A.n;
+  C.m = B.m;
+  C.ptr.assign(C.n + 1, 0);
+  std::vector<double> acc(B.m, 0.0);
+  std::vector<char> used(B.m, 0);
+  std::vector<int64_t> touched;
+  for (int64_t i = 0; i < A.n; ++i) {
+    touched.clear();
+    for (int64_t e = A.ptr[i]; e < A.ptr[i + 1]; ++e) {
+      const int64_t k = A.idx[e];
+      const double a = A.val[e];
+      for (int64_t f = B.ptr[k]; f < B.ptr[k + 1]; ++f) {
+        const int64_t j = B.idx[f];
+        if (!used[j]) { used[j] = 1; touched.push_back(j); acc[j] = 0.0; }
+        acc[j] += a * B.val[f];
+      }
+    }
+    std::sort(touched.begin(), touched.end());
+    double mx = 0;
+    for (int64_t j : touched) mx = std::max(mx, std::fabs(acc[j]));
+    for (int64_t j : touched) {
+      if (acc[j] != 0.0 && std::fabs(acc[j]) > rel_drop * mx) {
+        C.idx.push_back(j);
+        C.val.push_back(acc[j]);
+      }
+      used[j] = 0;
+    }
+    C.ptr[i + 1] = (int64_t)C.idx.size();
+  }
+  return C;
+}
+
+Csr spadd(const Csr& A, double alpha, const Csr& B, double beta) {
+  Csr C;
+  C.n = A.n;
+  C.m = A.m;
+  C.ptr.assign(C.n + 1, 0);
+  for (int64_t i = 0; i < A.n; ++i) {
+    int64_t a = A.ptr[i], b = B.ptr[i];
+    while (a < A.ptr[i + 1] || b < B.ptr[i + 1]) {
+      int64_t ca = a < A.ptr[i + 1] ? A.idx[a] : INT64_MAX;
+      int64_t cb = b < B.ptr[i + 1] ? B.idx[b] : INT64_MAX;
+      double v;
+      int64_t c;
+      if (ca == cb) { c = ca; v = alpha * A.val[a++] + beta * B.val[b++]; }
+      else if (ca < cb) { c = ca; v = alpha * A.val[a++]; }
+      else { c = cb; v = beta * B.val[b++]; }
+      if (v != 0.0) { C.idx.push_back(c); C.val.push_back(v); }
+    }
+    C.ptr[i + 1] = (int64_t)C.idx.size();
+  }
+  return C;
+}
+
+Csr identity(int64_t n) {
+  Csr I;
+  I.n = I.m = n;
+  I.ptr.resize(n + 1);
+  for (int64_t i = 0; i <= n; ++i) I.ptr[i] = i;
+  I.idx.resize(n);
+  std::iota(I.idx.begin(), I.idx.end(), 0);
+  I.val.assign(n, 1.0);
+  return I;
+}
+
+double max_abs(const Csr& A) {
+  double m = 0;
+  for (double v : A.val) m = std::max(m, std::fabs(v));
+  return m;
+}
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t alloc(size_t count) {
+    if (p) { cudaFree(p); p = nullptr; }
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, count * sizeof(T));
+  }
+  cudaError_t upload(const std::vector<T>& h) {
+    cudaError_t e = alloc(h.size());
+    if (e != cudaSuccess || h.empty()) return e;
+    return cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+
+}  // namespace
+
+struct bfe_plan {
+  int64_t n = 0;
+  int32_t mode = 0, prec = 0;
+  double dt = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // operator
+  int32_t n_slices = 0;
+  int32_t max_slice_entries = 0;
+  DevBuf<int32_t> slice_ptr;
+  DevBuf<uint32_t> col;
+  DevBuf<unsigned char> val;        // double or float
+  DevBuf<unsigned char> rowc;       // double or float
+  std::vector<uint32_t> h_base;     // node-block base per row
+  std::vector<double> h_acoef;      // forcing coefficient per row (diagonal of A)
+  // interface correction
+  int32_t n_int = 0;
+  int32_t int_base_prev = 1;
+  std::vector<int32_t> h_int_row;
+  DevBuf<int32_t> int_row, z_ptr, z_col;
+  DevBuf<unsigned char> z_val;
+  // statistics
+  int64_t nnz_operator = 0;         // stored (unpadded) entries
+  int64_t n_direct_rows = 0;
+};
+
+namespace {
+
+size_t elem_size(int prec) { return prec == BFE_PREC_DOUBLE ? sizeof(double) : sizeof(float); }
+
+template <typename T>
+void push_val(std::vector<unsigned char>& buf, double v) {
+  T x = (T)v;
+  const unsigned char* b = reinterpret_cast<const unsigned char*>(&x);
+  buf.insert(buf.end(), b, b + sizeof(T));
+}
+
+int upload_bytes(DevBuf<unsigned char>& d, const std::vector<unsigned char>& h) {
+  CUDA_TRY(d.upload(h));
+  return BFE_OK;
+}
+
+// Build the interface correction operator over the rows coupled by the
+// off-diagonal part of C. For 'vel at curent time step' the implicit system
+// (I + Q) w = v with Q = P_d^-1 dt/2 M^-1 C_off is solved exactly by
+// Z = (I - Q) (I + Q^2 + Q^4 + ...), truncated when the next term is below
+// tol relative to the sum; for 'vel at last half time step' the explicit
+// correction is Z = -dt M^-1 C_off.
+int build_interface(bfe_plan* pl, const Csr& Coff, const std::vector<double>& m,
+                    const std::vector<double>& pdiag, std::vector<int32_t>& int_rows,
+                    Csr& Z) {
+  std::vector<char> is_int(pl->n, 0);
+  for (int64_t i = 0; i < Coff.n; ++i)
+    for (int64_t e = Coff.ptr[i]; e < Coff.ptr[i + 1]; ++e) { is_int[i] = 1; is_int[Coff.idx[e]] = 1; }
+  int_rows.clear();
+  std::vector<int64_t> loc(pl->n, -1);
+  for (int64_t i = 0; i < pl->n; ++i)
+    if (is_int[i]) { loc[i] = (int64_t)int_rows.size(); int_rows.push_back((int32_t)i); }
+  const int64_t ni = (int64_t)int_rows.size();
+  Csr Q;
+  Q.n = Q.m = ni;
+  Q.ptr.assign(ni + 1, 0);
+  const double dt = pl->dt;
+  for (int64_t t = 0; t < ni; ++t) {
+    const int64_t i = int_rows[t];
+    std::vector<std::pair<int64_t, double>> row;
+    for (int64_t e = Coff.ptr[i]; e < Coff.ptr[i + 1]; ++e) {
+      const double g = dt / 2 * Coff.val[e] / m[i];
+      const double v = pl->mode == BFE_MODE_VEL_CURRENT ? pdiag[i] * g : -2.0 * g;
+      row.emplace_back(loc[Coff.idx[e]], v);
+    }
+    std::sort(row.begin(), row.end());
+    for (auto& x : row) { Q.idx.push_back(x.first); Q.val.push_back(x.second); }
+    Q.ptr[t + 1] = (int64_t)Q.idx.size();
+  }
+  if (pl->mode != BFE_MODE_VEL_CURRENT) {
+    Z = Q;           // u_new = u_hat + (-dt M^-1 C_off)(u_n - u_{n-1})
+    return BFE_OK;
+  }
+  const double tol = pl->prec == BFE_PREC_DOUBLE ? 1e-18 : 1e-10;
+  Csr S = spgemm(Q, Q, 0.0);
+  Csr I = identity(ni);
+  Csr acc = I, T = I;
+  bool conv = false;
+  for (int it = 0; it < 64; ++it) {
+    T = spgemm(S, T, tol * 1e-3);
+    const double tm = max_abs(T);
+    acc = spadd(acc, 1.0, T, 1.0);
+    if (tm <= tol * max_abs(acc)) { conv = true; break; }
+  }
+  if (!conv)
+    return fail(BFE_ERR_UNSUPPORTED,
+                "fluid-solid coupling series did not converge: the coupled step is not "
+                "dominated by the diagonal (check dt and the interface element matrices)");
+  Csr ImQ = spadd(I, 1.0, Q, -1.0);
+  Z = spgemm(ImQ, acc, tol * 1e-3);
+  return BFE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bfe_last_error(void) { return g_last_error.c_str(); }
+
+int bfe_version(int32_t* major, int32_t* minor, int32_t* patch) {
+  if (major) *major = 0;
+  if (minor) *minor = 1;
+  if (patch) *patch = 0;
+  return BFE_OK;
+}
+
+int bfe_plan_ndof(const bfe_plan* plan, int64_t* n) {
+  if (!plan || !n) return fail(BFE_ERR_ARG, "NULL argument");
+  *n = plan->n;
+  return BFE_OK;
+}
+
+int bfe_plan_destroy(bfe_plan* plan) {
+  if (!plan) return BFE_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaSetDevice(plan->device);
+  if (plan->stream) cudaStreamDestroy(plan->stream);
+  delete plan;
+  cudaSetDevice(dev);
+  return BFE_OK;
+}
+
+int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse* Mv,
+                    double dt, int32_t solver_mode, int32_t precision,
+                    const int64_t* dof_node, const int32_t* dof_type, bfe_plan** out) {
+  g_last_error.clear();
+  if (!out) return fail(BFE_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (solver_mode != BFE_MODE_VEL_CURRENT && solver_mode != BFE_MODE_VEL_LAST_HALF)
+    return fail(BFE_ERR_ARG, "unknown solver_mode %d", solver_mode);
+  if (precision != BFE_PREC_DOUBLE && precision != BFE_PREC_SINGLE)
+    return fail(BFE_ERR_ARG, "unknown precision %d", precision);
+  if (!(dt > 0) || !std::isfinite(dt)) return fail(BFE_ERR_ARG, "dt must be positive and finite");
+  Csr K, C, M;
+  int rc;
+  if ((rc = to_csr(Kv, "K", K))) return rc;
+  if ((rc = to_csr(Cv, "C", C))) return rc;
+  if ((rc = to_csr(Mv, "M", M))) return rc;
+  if (K.n != K.m) return fail(BFE_ERR_ARG, "K must be square matrix");
+  if (C.n != C.m) return fail(BFE_ERR_ARG, "C must be square matrix");
+  if (M.n != M.m) return fail(BFE_ERR_ARG, "M must be square matrix");
+  if (C.n != K.n || M.n != K.n) return fail(BFE_ERR_ARG, "K, C and M must have the same size");
+  const int64_t n = K.n;
+  if (n == 0) return fail(BFE_ERR_ARG, "empty model");
+  if (n > bfe::kMaxDof) return fail(BFE_ERR_UNSUPPORTED, "more than %lld DOFs", (long long)bfe::kMaxDof);
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    return fail(BFE_ERR_NO_DEVICE, "no CUDA device available");
+
+  std::unique_ptr<bfe_plan> pl(new bfe_plan());
+  pl->n = n;
+  pl->mode = solver_mode;
+  pl->prec = precision;
+  pl->dt = dt;
+  CUDA_TRY(cudaGetDevice(&pl->device));
+
+  // lumped mass: sum(M).' = column sums (v6.m:122-123)
+  std::vector<double> m(n, 0.0);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t e = M.ptr[i]; e < M.ptr[i + 1]; ++e) m[M.idx[e]] += M.val[e];
+  for (int64_t i = 0; i < n; ++i)
+    if (m[i] == 0.0 || !std::isfinite(m[i]))
+      return fail(BFE_ERR_NUMERIC, "DOF %lld has zero lumped mass", (long long)i);
+
+  // split C into its diagonal and the off-diagonal (interface) part
+  std::vector<double> cdiag(n, 0.0);
+  Csr Coff;
+  Coff.n = Coff.m = n;
+  Coff.ptr.assign(n + 1, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    for (int64_t e = C.ptr[i]; e < C.ptr[i + 1]; ++e) {
+      if (C.idx[e] == i) cdiag[i] += C.val[e];
+      else { Coff.idx.push_back(C.idx[e]); Coff.val.push_back(C.val[e]); }
+    }
+    Coff.ptr[i + 1] = (int64_t)Coff.idx.size();
+  }
+
+  // per-row coefficients (v6.m:130-139 with the diagonal part of P)
+  std::vector<double> pdiag(n), rowc(n), acoef(n), lscale(n);
+  for (int64_t i = 0; i < n; ++i) {
+    const double g = dt / 2 * cdiag[i] / m[i];
+    if (solver_mode == BFE_MODE_VEL_CURRENT) {
+      const double p = 1.0 / (1.0 + g);
+      pdiag[i] = p;
+      acoef[i] = p * dt * dt / m[i];
+      lscale[i] = p * dt * dt / m[i];
+      rowc[i] = precision == BFE_PREC_DOUBLE ? p * (-1.0 + g) : (1.0 - g) / (1.0 + g);
+    } else {
+      pdiag[i] = 1.0;
+      acoef[i] = dt * dt / m[i];
+      lscale[i] = dt * dt / m[i];
+      rowc[i] = precision == BFE_PREC_DOUBLE ? (2.0 * g - 1.0) : (1.0 - 2.0 * g);
+    }
+  }
+
+  // node blocks for the FP32 difference form
+  std::vector<int64_t> blk_base(n, -1), blk_len(n, 0);
+  bool have_nodes = precision == BFE_PREC_SINGLE && dof_node && dof_type;
+  if (have_nodes) {
+    int64_t i = 0;
+    std::map<int64_t, int64_t> seen;
+    while (i < n && have_nodes) {
+      int64_t j = i;
+      while (j < n && dof_node[j] == dof_node[i]) ++j;
+      if (j - i > 8 || seen.count(dof_node[i])) { have_nodes = false; break; }
+      seen[dof_node[i]] = i;
+      for (int64_t k = i; k < j; ++k) { blk_base[k] = i; blk_len[k] = j - i; }
+      i = j;
+    }
+  }
+
+  // pack rows into the sliced ELL layout
+  const int64_t n_slices = (n + bfe::kSlice - 1) / bfe::kSlice;
+  pl->n_slices = (int32_t)n_slices;
+  std::vector<int32_t> sptr(n_slices + 1, 0);
+  std::vector<std::vector<std::pair<uint32_t, double>>> rows(bfe::kSlice);
+  std::vector<uint32_t> hcol;
+  std::vector<unsigned char> hval;
+  pl->h_base.assign(n, 0);
+  int64_t stored = 0, direct_rows = 0;
+  for (int64_t s = 0; s < n_slices; ++s) {
+    size_t w = 0;
+    for (int r = 0; r < bfe::kSlice; ++r) {
+      rows[r].clear();
+      const int64_t i = s * bfe::kSlice + r;
+      if (i >= n) continue;
+      if (precision == BFE_PREC_DOUBLE) {
+        bool has_diag = false;
+        for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
+          const int64_t j = K.idx[e];
+          double v = -lscale[i] * K.val[e];
+          if (j == i) {
+            v += solver_mode == BFE_MODE_VEL_CURRENT ? 2.0 * pdiag[i] : (2.0 - dt * cdiag[i] / m[i]);
+            has_diag = true;
+          }
+          rows[r].emplace_back((uint32_t)j, v);
+        }
+        if (!has_diag) {
+          const double v = solver_mode == BFE_MODE_VEL_CURRENT ? 2.0 * pdiag[i] : (2.0 - dt * cdiag[i] / m[i]);
+          rows[r].emplace_back((uint32_t)i, v);
+          std::sort(rows[r].begin(), rows[r].end());
+        }
+      } else {
+        // difference form if every column's DOF type exists in the row's
+        // node block and every per-type partial row sum of K vanishes
+        bool diff = have_nodes;
+        if (diff) {
+          std::map<int32_t, std::pair<double, double>> sums;  // type -> (sum, abs sum)
+          for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
+            auto& sm = sums[dof_type[K.idx[e]]];
+            sm.first += K.val[e];
+            sm.second += std::fabs(K.val[e]);
+          }
+          for (auto& kv : sums) {
+            bool found = false;
+            for (int64_t k = blk_base[i]; k < blk_base[i] + blk_len[i]; ++k)
+              if (dof_type[k] == kv.first) found = true;
+            if (!found || std::fabs(kv.second.first) > 1e-9 * kv.second.second) diff = false;
+          }
+        }
+        if (diff) {
+          pl->h_base[i] = (uint32_t)blk_base[i];
+          for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
+            const int64_t j = K.idx[e];
+            if (dof_node[j] == dof_node[i]) continue;   // own node block cancels
+            uint32_t slot = 0;
+            for (int64_t k = blk_base[i]; k < blk_base[i] + blk_len[i]; ++k)
+              if (dof_type[k] == dof_type[j]) slot = (uint32_t)(k - blk_base[i]);
+            rows[r].emplace_back((uint32_t)j | (slot << bfe::kSlotShift), lscale[i] * K.val[e]);
+          }
+        } else {
+          ++direct_rows;
+          for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e)
+            rows[r].emplace_back((uint32_t)K.idx[e] | bfe::kDirect, lscale[i] * K.val[e]);
+        }
+      }
+      stored += (int64_t)rows[r].size();
+      w = std::max(w, rows[r].size());
+    }
+    for (size_t k = 0; k < w; ++k) {
+      for (int r = 0; r < bfe::kSlice; ++r) {
+        const int64_t i = s * bfe::kSlice + r;
+        uint32_t c;
+        double v;
+        if (k < rows[r].size()) { c = rows[r][k].first; v = rows[r][k].second; }
+        else { c = (uint32_t)std::min<int64_t>(i, n - 1) | (precision == BFE_PREC_SINGLE ? bfe::kDirect : 0u); v = 0.0; }
+        hcol.push_back(c);
+        if (precision == BFE_PREC_DOUBLE) push_val<double>(hval, v); else push_val<float>(hval, v);
+      }
+    }
+    sptr[s + 1] = (int32_t)hcol.size();
+    if (hcol.size() > (size_t)INT32_MAX) return fail(BFE_ERR_UNSUPPORTED, "operator too large for 32-bit offsets");
+    pl->max_slice_entries = std::max<int32_t>(pl->max_slice_entries, (int32_t)(w * bfe::kSlice));
+  }
+  pl->nnz_operator = stored;
+  pl->n_direct_rows = direct_rows;
+  pl->h_acoef = acoef;
+
+  // interface correction
+  Csr Z;
+  std::vector<int32_t> irows;
+  if (Coff.idx.size()) {
+    if ((rc = build_interface(pl.get(), Coff, m, pdiag, irows, Z))) return rc;
+  }
+  pl->n_int = (int32_t)irows.size();
+  pl->int_base_prev = solver_mode == BFE_MODE_VEL_CURRENT ? 1 : 0;
+  pl->h_int_row = irows;
+
+  // upload
+  CUDA_TRY(pl->slice_ptr.upload(sptr));
+  CUDA_TRY(pl->col.upload(hcol));
+  if ((rc = upload_bytes(pl->val, hval))) return rc;
+  std::vector<unsigned char> hrc;
+  for (int64_t i = 0; i < n; ++i) {
+    if (precision == BFE_PREC_DOUBLE) push_val<double>(hrc, rowc[i]); else push_val<float>(hrc, rowc[i]);
+  }
+  if ((rc = upload_bytes(pl->rowc, hrc))) return rc;
+  if (pl->n_int) {
+    std::vector<int32_t> zp(Z.ptr.begin(), Z.ptr.end()), zc(Z.idx.begin(), Z.idx.end());
+    std::vector<unsigned char> zv;
+    for (double v : Z.val) { if (precision == BFE_PREC_DOUBLE) push_val<double>(zv, v); else push_val<float>(zv, v); }
+    CUDA_TRY(pl->int_row.upload(irows));
+    CUDA_TRY(pl->z_ptr.upload(zp));
+    CUDA_TRY(pl->z_col.upload(zc));
+    if ((rc = upload_bytes(pl->z_val, zv))) return rc;
+  }
+  CUDA_TRY(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
+  *out = pl.release();
+  return BFE_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Run machinery shared by bfe_run, bfe_run_batched and bfe_run_device.
+namespace {
+
+struct ForceEntry {
+  int32_t row, rhs, sig;
+  double w;
+};
+
+struct RunSpec {
+  int64_t R = 1, n_t = 0, ti_start = 0;
+  std::vector<ForceEntry> frc;     // one per (row, rhs) after last-wins dedupe
+  int64_t n_sig = 0;
+  const double* d_sig64 = nullptr; // device [n_t][n_sig]
+  std::vector<int64_t> hist_idx;
+  double* d_hist = nullptr;        // device [q][n_t][R] column-major (slot fastest)
+  int64_t every_n = 0;             // R == 1 only
+  int32_t field_is_vel = 1;
+  double* d_fld = nullptr;
+  std::vector<double>* fld_time = nullptr;
+  const double* time = nullptr;    // host time samples (for frame times)
+};
+
+int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
+  const int64_t n = pl->n, R = rs.R;
+  const int prec = pl->prec;
+  const size_t es = elem_size(prec);
+  if ((double)n * (double)R > 4.0e12) return fail(BFE_ERR_ARG, "state too large");
+  // forcing list sorted by (row, rhs)
+  std::sort(rs.frc.begin(), rs.frc.end(), [](const ForceEntry& a, const ForceEntry& b) {
+    return a.row != b.row ? a.row < b.row : a.rhs < b.rhs;
+  });
+  std::vector<int32_t> frow, frhs, fsig;
+  std::vector<unsigned char> fcoef;
+  for (auto& f : rs.frc) {
+    frow.push_back(f.row);
+    frhs.push_back(f.rhs);
+    fsig.push_back(f.sig);
+    const double c = pl->h_acoef[f.row] * f.w;
+    if (prec == BFE_PREC_DOUBLE) push_val<double>(fcoef, c); else push_val<float>(fcoef, c);
+  }
+  // monitors sorted by row
+  std::vector<std::pair<int32_t, int32_t>> mons;
+  for (size_t k = 0; k < rs.hist_idx.size(); ++k) mons.emplace_back((int32_t)rs.hist_idx[k], (int32_t)k);
+  std::sort(mons.begin(), mons.end());
+  std::vector<int32_t> mrow, mslot;
+  for (auto& x : mons) { mrow.push_back(x.first); mslot.push_back(x.second); }
+  // per-row info word for this run
+  std::vector<uint32_t> info(pl->h_base);
+  for (auto& f : rs.frc) info[f.row] |= bfe::kRowForced;
+  for (auto& x : mons) info[x.first] |= bfe::kRowMonitored;
+  for (int32_t r : pl->h_int_row) info[r] |= bfe::kRowInterface;
+
+  DevBuf<int32_t> d_frow, d_frhs, d_fsig, d_mrow, d_mslot;
+  DevBuf<unsigned char> d_fcoef, d_u, d_vint;
+  DevBuf<uint32_t> d_info;
+  DevBuf<float> d_sig32;
+  CUDA_TRY(d_frow.upload(frow));
+  CUDA_TRY(d_frhs.upload(frhs));
+  CUDA_TRY(d_fsig.upload(fsig));
+  CUDA_TRY(d_fcoef.upload(fcoef));
+  CUDA_TRY(d_mrow.upload(mrow));
+  CUDA_TRY(d_mslot.upload(mslot));
+  CUDA_TRY(d_info.upload(info));
+  const void* dsig = rs.d_sig64;
+  if (prec == BFE_PREC_SINGLE && rs.n_sig > 0) {
+    CUDA_TRY(d_sig32.alloc((size_t)rs.n_t * rs.n_sig));
+    CUDA_TRY(bfe::launch_cast_f64_to_f32(rs.d_sig64, d_sig32.p, rs.n_t * rs.n_sig, st));
+    dsig = d_sig32.p;
+  }
+  const size_t state_bytes = (size_t)n * R * es;
+  CUDA_TRY(d_u.alloc(3 * state_bytes));
+  CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * state_bytes, st));
+  if (pl->n_int) {
+    CUDA_TRY(d_vint.alloc((size_t)pl->n_int * R * es));
+  }
+  if (R > 1) {
+    const size_t smem = bfe::batched_smem_bytes(prec, pl->max_slice_entries);
+    if (smem > 227 * 1024) return fail(BFE_ERR_UNSUPPORTED, "operator rows too long for the batched kernel");
+    CUDA_TRY(bfe::set_batched_smem_limit(prec, std::max<size_t>(smem, 1)));
+  }
+
+  bfe::StepArgs a{};
+  a.n = (int32_t)n;
+  a.R = (int32_t)R;
+  a.n_slices = pl->n_slices;
+  a.slice_ptr = pl->slice_ptr.p;
+  a.col = pl->col.p;
+  a.val = pl->val.p;
+  a.rowc = pl->rowc.p;
+  a.rowinfo = d_info.p;
+  a.n_frc = (int32_t)frow.size();
+  a.frc_row = d_frow.p;
+  a.frc_rhs = d_frhs.p;
+  a.frc_sig = d_fsig.p;
+  a.frc_coef = d_fcoef.p;
+  a.sig = dsig;
+  a.n_sig = (int32_t)rs.n_sig;
+  a.n_mon = (int32_t)mrow.size();
+  a.mon_row = d_mrow.p;
+  a.mon_slot = d_mslot.p;
+  a.q = (int32_t)rs.hist_idx.size();
+  a.n_t = rs.n_t;
+  a.hist = rs.d_hist;
+  a.n_int = pl->n_int;
+  a.int_row = pl->int_row.p;
+  a.z_ptr = pl->z_ptr.p;
+  a.z_col = pl->z_col.p;
+  a.z_val = pl->z_val.p;
+  a.int_base_prev = pl->int_base_prev;
+  a.v_int = d_vint.p;
+  unsigned char* U[3] = {d_u.p, d_u.p + state_bytes, d_u.p + 2 * state_bytes};
+  int iprev = 0, icur = 1, inew = 2;
+  for (int64_t ti = rs.ti_start; ti < rs.n_t; ++ti) {
+    a.ti = ti;
+    a.u_prev = U[iprev];
+    a.u_n = U[icur];
+    a.u_new = U[inew];
+    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
+                           : bfe::launch_step_batched(a, prec, pl->max_slice_entries, st);
+    if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
+    if (pl->n_int) {
+      e = bfe::launch_interface_fixup(a, prec, st);
+      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "interface kernel launch failed: %s", cudaGetErrorString(e));
+    }
+    if (rs.every_n > 0 && rs.d_fld && ti % rs.every_n == 0) {
+      const int64_t k = ti / rs.every_n;
+      e = bfe::launch_frame(a, prec, rs.d_fld, k, rs.field_is_vel, pl->dt, st);
+      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "frame kernel launch failed: %s", cudaGetErrorString(e));
+      if (rs.fld_time) (*rs.fld_time)[k] = rs.time[ti];
+    }
+    const int t = iprev;
+    iprev = icur;
+    icur = inew;
+    inew = t;
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return BFE_OK;
+}
+
+// First 0-based column with any non-zero |forcing| (v6.m:163-169); n_t if none.
+int64_t first_nonzero_column(const double* frcs, int64_t rows, int64_t n_t, int64_t R) {
+  for (int64_t ti = 0; ti < n_t; ++ti)
+    for (int64_t r = 0; r < R; ++r)
+      for (int64_t k = 0; k < rows; ++k)
+        if (frcs[k + rows * (ti + n_t * r)] != 0.0) return ti;
+  return n_t;
+}
+
+int check_time(bfe_plan* pl, int64_t n_t, const double* time) {
+  if (n_t < 2 || !time) return fail(BFE_ERR_ARG, "time must have at least 2 samples");
+  const double dt = time[1] - time[0];
+  if (std::fabs(dt - pl->dt) > 1e-9 * std::fabs(pl->dt))
+    return fail(BFE_ERR_ARG, "time step %.17g differs from the plan's dt %.17g", dt, pl->dt);
+  return BFE_OK;
+}
+
+// Build forcing entries with MATLAB last-wins semantics per (rhs, dof).
+int build_forcing(bfe_plan* pl, int64_t R, int64_t p, const int64_t* frc_idx, int64_t frc_rows,
+                  std::vector<ForceEntry>& out) {
+  if (p > 0 && !frc_idx) return fail(BFE_ERR_ARG, "frc_idx is NULL");
+  if (p > 0 && frc_rows != 1 && frc_rows != p)
+    return fail(BFE_ERR_ARG, "forcing_functions must have 1 or %lld rows, got %lld", (long long)p, (long long)frc_rows);
+  out.clear();
+  for (int64_t r = 0; r < R; ++r) {
+    std::map<int64_t, int64_t> last;   // dof -> slot
+    for (int64_t e = 0; e < p; ++e) {
+      const int64_t d = frc_idx[e + p * r];
+      if (d < 0 && R > 1) continue;    // padding of ragged source sets
+      if (d < 0 || d >= pl->n) return fail(BFE_ERR_ARG, "forcing index %lld out of range", (long long)d);
+      last[d] = e;
+    }
+    for (auto& kv : last) {
+      const int64_t sig = (frc_rows == 1 ? 0 : kv.second) + frc_rows * r;
+      out.push_back({(int32_t)kv.first, (int32_t)r, (int32_t)sig, 1.0});
+    }
+  }
+  return BFE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bfe_run_batched(bfe_plan* plan, int64_t R, int64_t n_t, const double* time,
+                    int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+                    int64_t q, const int64_t* hist_idx, double* hist_out) {
+  g_last_error.clear();
+  if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
+  if (R < 1) return fail(BFE_ERR_ARG, "R must be >= 1");
+  int rc;
+  if ((rc = check_time(plan, n_t, time))) return rc;
+  if (q < 0 || p < 0) return fail(BFE_ERR_ARG, "negative sizes");
+  if (q > 0 && (!hist_idx || !hist_out)) return fail(BFE_ERR_ARG, "hist_idx/hist_out is NULL");
+  for (int64_t k = 0; k < q; ++k)
+    if (hist_idx[k] < 0 || hist_idx[k] >= plan->n) return fail(BFE_ERR_ARG, "history index %lld out of range", (long long)hist_idx[k]);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != plan->device) CUDA_TRY(cudaSetDevice(plan->device));
+  RunSpec rs;
+  rs.R = R;
+  rs.n_t = n_t;
+  rs.time = time;
+  if ((rc = build_forcing(plan, R, p, frc_idx, frc_rows, rs.frc))) return rc;
+  rs.ti_start = (p > 0 && frcs) ? first_nonzero_column(frcs, frc_rows, n_t, R) : n_t;
+  if (p > 0 && !frcs) return fail(BFE_ERR_ARG, "frcs is NULL");
+  rs.hist_idx.assign(hist_idx, hist_idx + q);
+  cudaStream_t st = plan->stream;
+  DevBuf<double> d_sig, d_hist;
+  rs.n_sig = p > 0 ? frc_rows * R : 0;
+  if (rs.n_sig) {
+    // host frcs is frc_rows x n_t x R (column-major) -> device [n_t][n_sig]
+    std::vector<double> h((size_t)n_t * rs.n_sig);
+    for (int64_t r = 0; r < R; ++r)
+      for (int64_t ti = 0; ti < n_t; ++ti)
+        for (int64_t k = 0; k < frc_rows; ++k)
+          h[(size_t)ti * rs.n_sig + k + frc_rows * r] = frcs[k + frc_rows * (ti + n_t * r)];
+    CUDA_TRY(d_sig.upload(h));
+    rs.d_sig64 = d_sig.p;
+  }
+  const size_t hist_n = (size_t)q * n_t * R;
+  CUDA_TRY(d_hist.alloc(hist_n));
+  if (hist_n) CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
+  rs.d_hist = d_hist.p;
+  if ((rc = execute(plan, rs, st))) return rc;
+  if (hist_n) {
+    CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (dev != plan->device) cudaSetDevice(dev);
+  return BFE_OK;
+}
+
+int bfe_run(bfe_plan* plan, int64_t n_t, const double* time,
+            int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+            int64_t q, const int64_t* hist_idx, int64_t every_n, int32_t field_is_vel,
+            double* hist_out, double* fld_out, double* fld_time_out) {
+  g_last_error.clear();
+  if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
+  if (every_n <= 0) {
+    return bfe_run_batched(plan, 1, n_t, time, p, frc_idx, frc_rows, frcs, q, hist_idx, hist_out);
+  }
+  int rc;
+  if ((rc = check_time(plan, n_t, time))) return rc;
+  if (!fld_out || !fld_time_out) return fail(BFE_ERR_ARG, "fld_out/fld_time_out is NULL");
+  if (q < 0 || p < 0) return fail(BFE_ERR_ARG, "negative sizes");
+  if (q > 0 && (!hist_idx || !hist_out)) return fail(BFE_ERR_ARG, "hist_idx/hist_out is NULL");
+  for (int64_t k = 0; k < q; ++k)
+    if (hist_idx[k] < 0 || hist_idx[k] >= plan->n) return fail(BFE_ERR_ARG, "history index %lld out of range", (long long)hist_idx[k]);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != plan->device) CUDA_TRY(cudaSetDevice(plan->device));
+  RunSpec rs;
+  rs.R = 1;
+  rs.n_t = n_t;
+  rs.time = time;
+  if ((rc = build_forcing(plan, 1, p, frc_idx, frc_rows, rs.frc))) return rc;
+  if (p > 0 && !frcs) return fail(BFE_ERR_ARG, "frcs is NULL");
+  rs.ti_start = p > 0 ? first_nonzero_column(frcs, frc_rows, n_t, 1) : n_t;
+  rs.hist_idx.assign(hist_idx, hist_idx + q);
+  cudaStream_t st = plan->stream;
+  DevBuf<double> d_sig, d_hist, d_fld;
+  rs.n_sig = p > 0 ? frc_rows : 0;
+  if (rs.n_sig) {
+    std::vector<double> h((size_t)n_t * rs.n_sig);
+    for (int64_t ti = 0; ti < n_t; ++ti)
+      for (int64_t k = 0; k < frc_rows; ++k) h[(size_t)ti * rs.n_sig + k] = frcs[k + frc_rows * ti];
+    CUDA_TRY(d_sig.upload(h));
+    rs.d_sig64 = d_sig.p;
+  }
+  const size_t hist_n = (size_t)q * n_t;
+  CUDA_TRY(d_hist.alloc(hist_n));
+  if (hist_n) CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
+  rs.d_hist = d_hist.p;
+  const int64_t n_frames = (n_t + every_n - 1) / every_n;
+  CUDA_TRY(d_fld.alloc((size_t)plan->n * n_frames));
+  CUDA_TRY(cudaMemsetAsync(d_fld.p, 0, (size_t)plan->n * n_frames * sizeof(double), st));
+  std::vector<double> ftime(n_frames, 0.0);
+  rs.every_n = every_n;
+  rs.field_is_vel = field_is_vel;
+  rs.d_fld = d_fld.p;
+  rs.fld_time = &ftime;
+  if ((rc = execute(plan, rs, st))) return rc;
+  if (hist_n) CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(fld_out, d_fld.p, (size_t)plan->n * n_frames * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
+  if (dev != plan->device) cudaSetDevice(dev);
+  return BFE_OK;
+}
+
+int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
+                   int64_t n_frc, const int64_t* frc_dof, const int64_t* frc_rhs,
+                   const int64_t* frc_sig, const double* frc_w,
+                   int64_t n_sig, const double* d_sig,
+                   int64_t q, const int64_t* hist_idx, double* d_hist, void* stream) {
+  g_last_error.clear();
+  if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
+  if (R < 1 || n_t < 1 || ti_start < 0 || n_frc < 0 || n_sig < 0 || q < 0)
+    return fail(BFE_ERR_ARG, "invalid sizes");
+  if (n_frc > 0 && (!frc_dof || !frc_rhs || !frc_sig || !d_sig)) return fail(BFE_ERR_ARG, "NULL forcing arrays");
+  if (q > 0 && (!hist_idx || !d_hist)) return fail(BFE_ERR_ARG, "NULL history arrays");
+  RunSpec rs;
+  rs.R = R;
+  rs.n_t = n_t;
+  rs.ti_start = std::min(ti_start, n_t);
+  std::map<std::pair<int64_t, int64_t>, size_t> seen;
+  for (int64_t e = 0; e < n_frc; ++e) {
+    if (frc_dof[e] < 0 || frc_dof[e] >= plan->n || frc_rhs[e] < 0 || frc_rhs[e] >= R ||
+        frc_sig[e] < 0 || frc_sig[e] >= n_sig)
+      return fail(BFE_ERR_ARG, "forcing entry %lld out of range", (long long)e);
+    const auto key = std::make_pair(frc_dof[e], frc_rhs[e]);
+    ForceEntry fe{(int32_t)frc_dof[e], (int32_t)frc_rhs[e], (int32_t)frc_sig[e], frc_w ? frc_w[e] : 1.0};
+    auto it = seen.find(key);
+    if (it != seen.end()) rs.frc[it->second] = fe;       // last wins
+    else { seen[key] = rs.frc.size(); rs.frc.push_back(fe); }
+  }
+  for (int64_t k = 0; k < q; ++k)
+    if (hist_idx[k] < 0 || hist_idx[k] >= plan->n) return fail(BFE_ERR_ARG, "history index out of range");
+  rs.hist_idx.assign(hist_idx, hist_idx + q);
+  rs.n_sig = n_sig;
+  rs.d_sig64 = d_sig;
+  rs.d_hist = d_hist;
+  return execute(plan, rs, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+/*
+ * bfe_gb300.h - C ABI of the GB300-native explicit time-marching solver.
+ *
+ * This library replaces the per-load-step time-marching call of
+ * BristolFE-v2, i.e. the call
+ *
+ *     [history_output, field_output, force_output, field_output_time] = ...
+ *         fn_explicit_dynamic_solver_v6(K, C, M, time, forcing_indices,
+ *             forcing_functions, disp_indices, disp_functions,
+ *             history_indices, field_output_every_n_frames, use_gpu,
+ *             field_output_type, solver_mode, solver_precision)
+ *
+ * made from code/fn_BristolFE_v2.m:120-122 (interface defined at
+ * code/internal/fn_explicit_dynamic_solver_v6.m:1-5). The MATLAB side keeps
+ * the global assembly; a MEX gateway converts the MATLAB sparse matrices to
+ * bfe_sparse views (0-based) and calls bfe_plan_create + bfe_run.
+ *
+ * Conventions
+ *  - Every function returns an int status (BFE_OK = 0); on failure
+ *    bfe_last_error() returns a message for the calling thread. No
+ *    exception or exit() crosses this boundary.
+ *  - Indices are 0-based int64. Dense inputs/outputs are column-major
+ *    (MATLAB layout) and owned by the caller.
+ *  - A plan is not thread-safe; distinct plans may be used concurrently.
+ *  - All device-side waits are bounded; nothing here spins forever.
+ */
+#ifndef BFE_GB300_H
+#define BFE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BFE_OK 0
+#define BFE_ERR_ARG 1          /* invalid argument (sizes, indices, strings) */
+#define BFE_ERR_OOM 2          /* host or device allocation failed */
+#define BFE_ERR_CUDA 3         /* CUDA runtime error */
+#define BFE_ERR_NUMERIC 4      /* zero lumped mass, NaN/Inf in inputs */
+#define BFE_ERR_UNSUPPORTED 5  /* valid request the reference path rejects */
+#define BFE_ERR_NO_DEVICE 6    /* no usable GPU */
+
+/* sparse matrix storage formats */
+#define BFE_CSR 0              /* ptr = row pointers, idx = column indices  */
+#define BFE_CSC 1              /* ptr = column pointers, idx = row indices (MATLAB) */
+
+/* solver_mode strings of fn_explicit_dynamic_solver_v6.m:130-139 */
+#define BFE_MODE_VEL_CURRENT 0    /* 'vel at curent time step' (v6.m:135, default) */
+#define BFE_MODE_VEL_LAST_HALF 1  /* 'vel at last half time step' (v6.m:131) */
+
+/* solver_precision of v6.m:57-61,141-159 */
+#define BFE_PREC_DOUBLE 0      /* plain FP64 state and operator */
+#define BFE_PREC_SINGLE 1      /* FP32 operator and state, compensated update */
+
+/* A view of one sparse matrix (not copied beyond bfe_plan_create). */
+typedef struct bfe_sparse {
+  int64_t n_rows;
+  int64_t n_cols;
+  int64_t nnz;
+  int32_t format;          /* BFE_CSR or BFE_CSC */
+  const int64_t* ptr;      /* length (n_rows or n_cols) + 1 */
+  const int64_t* idx;      /* length nnz */
+  const double* val;       /* length nnz */
+} bfe_sparse;
+
+typedef struct bfe_plan bfe_plan;
+
+/*
+ * Build the time-stepping operators on the current CUDA device.
+ * Replaces the operator formation of fn_explicit_dynamic_solver_v6.m:122-159
+ * (lumped mass = column sums of M; A, B, D for the selected mode).
+ *
+ * dof_node / dof_type (optional, may be NULL) give, for every global DOF,
+ * an identifier of its node and its DOF number (1..4 in BristolFE). They are
+ * what fn_BristolFE_v2 holds in mats.gl_lookup (code/fn_BristolFE_v2.m:53-58).
+ * With them the FP32 plan evaluates the stiffness product in a
+ * translation-invariant difference form, which keeps FP32 A-scans within
+ * 1e-4 of FP64; without them the FP32 plan uses the direct form.
+ */
+int bfe_plan_create(const bfe_sparse* K, const bfe_sparse* C, const bfe_sparse* M,
+                    double dt, int32_t solver_mode, int32_t precision,
+                    const int64_t* dof_node, const int32_t* dof_type,
+                    bfe_plan** out);
+
+int bfe_plan_destroy(bfe_plan* plan);
+
+/* Number of global DOFs of a plan. */
+int bfe_plan_ndof(const bfe_plan* plan, int64_t* n);
+
+/*
+ * One load step, host buffers (the MEX path).
+ * Follows fn_explicit_dynamic_solver_v6.m:161-218:
+ *   time            n_t sample times; dt = time[1] - time[0] must equal the
+ *                   plan's dt
+ *   frc_idx[p]      forced DOFs; frcs is frc_rows x n_t with frc_rows = 1
+ *                   (broadcast to every forced DOF) or p; duplicate DOFs take
+ *                   the last row, like MATLAB indexed assignment
+ *   hist_idx[q]     monitored DOFs; hist_out is q x n_t
+ *   every_n         field output every n-th sample starting at the first
+ *                   (<= 0: none, MATLAB's inf); fld_out is n x n_frames,
+ *                   fld_time_out n_frames, n_frames = ceil(n_t / every_n)
+ *   field_is_vel    1: frames hold (u - u_prev) / dt, 0: frames hold u
+ * Samples before the first non-zero forcing column stay zero (v6.m:163-169).
+ * Prescribed displacements are not part of this call: the reference's v6
+ * path fails on them (v6.m:191 reads an undefined variable).
+ */
+int bfe_run(bfe_plan* plan, int64_t n_t, const double* time,
+            int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+            int64_t q, const int64_t* hist_idx,
+            int64_t every_n, int32_t field_is_vel,
+            double* hist_out, double* fld_out, double* fld_time_out);
+
+/*
+ * R independent load steps sharing one operator (array full-matrix capture:
+ * one step per transmitter, subdoms/fn_run_main_model.m:101-115), run as one
+ * multi-right-hand-side time march. Host buffers.
+ *   frc_idx   p x R (column r lists the forced DOFs of source r; -1 pads)
+ *   frcs      frc_rows x n_t x R, frc_rows = 1 or p
+ *   hist_out  q x n_t x R (the same q monitored DOFs for every source)
+ */
+int bfe_run_batched(bfe_plan* plan, int64_t R, int64_t n_t, const double* time,
+                    int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+                    int64_t q, const int64_t* hist_idx, double* hist_out);
+
+/*
+ * Device-resident variant of bfe_run_batched for callers that keep inputs
+ * and outputs in GPU memory (no host copies). Pointers named d_* are device
+ * pointers:
+ *   d_sig    FP64 signals, n_sig values per time sample, time-major
+ *            (d_sig[ti * n_sig + k])
+ *   d_hist   FP64 history q x n_t x R, column-major like hist_out of
+ *            bfe_run_batched; the caller zeroes it (samples before ti_start
+ *            are not written)
+ * The forcing map (which signal drives which DOF of which source, and with
+ * what weight) is given on the host and copied once per call:
+ *   frc_dof[e], frc_rhs[e], frc_sig[e], frc_w[e] (NULL = 1.0) for e < n_frc
+ * ti_start is the first sample to compute (0-based).
+ * stream is a cudaStream_t (NULL = legacy default stream); the call returns
+ * after the work on it has finished.
+ */
+int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
+                   int64_t n_frc, const int64_t* frc_dof, const int64_t* frc_rhs,
+                   const int64_t* frc_sig, const double* frc_w,
+                   int64_t n_sig, const double* d_sig,
+                   int64_t q, const int64_t* hist_idx, double* d_hist,
+                   void* stream);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* bfe_last_error(void);
+
+/* Library version. */
+int bfe_version(int32_t* major, int32_t* minor, int32_t* patch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BFE_GB300_H */

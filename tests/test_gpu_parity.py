@@ -1,0 +1,170 @@
+"""GPU parity: the native kernels (through the C ABI) against the FP64 oracle.
+
+Tolerances: max-normalised error max|gpu - oracle| / max|oracle| of each
+result, <= 1e-10 for FP64 plans and <= 1e-4 for FP32 plans (the acceptance
+bound for FP32 A-scans)."""
+import numpy as np
+import pytest
+
+import modelgen
+from oracle import solver as osolver
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL32 = 1e-4
+
+
+def _err(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def bfe():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from bfe_gb300 import _lib, build
+    build.build()
+    import bfe_gb300
+    bfe_gb300.load()
+    return bfe_gb300
+
+
+def _oracle(m, t, fi, F, hi, every=np.inf, ftype="KE", mode=osolver.VEL_CURRENT):
+    return osolver.explicit_dynamic_solver_v6(m["K"], m["C"], m["M"], t, fi, F, [], [], hi,
+                                              every, 0, ftype, mode)
+
+
+@pytest.fixture(scope="module")
+def plate():
+    return modelgen.solid_plate(W=4e-3, H=2e-3, h=0.1e-3, dof_to_use=(1, 2))
+
+
+@pytest.fixture(scope="module")
+def coupled():
+    return modelgen.coupled_model(W=3e-3, Hw=1.5e-3, Hs=1.5e-3, h=0.1e-3, abs_thick=0.6e-3, blob=True)
+
+
+@pytest.mark.parametrize("prec,tol", [("double", TOL64), ("single", TOL32)])
+def test_solid_plate_history_and_frames(bfe, plate, prec, tol):
+    m = plate
+    nt = 700
+    t, s = modelgen.pulse(nt, m["dt"])
+    fi = modelgen.gi_of(m["gl"], [m["frc_nd"]], 2)
+    hi = modelgen.gi_of(m["gl"], m["mon_nds"], 2)
+    h0, f0, _, ft0 = _oracle(m, t, fi, s, hi, every=175)
+    h1, f1, frc, ft1 = bfe.fn_explicit_dynamic_solver_gb300(
+        m["K"], m["C"], m["M"], t, fi, s, [], [], hi, 175, 1, "KE", osolver.VEL_CURRENT, prec,
+        gl_lookup=m["gl"])
+    assert frc is None
+    assert h1.shape == h0.shape and f1.shape == f0.shape
+    assert _err(h1, h0) <= tol
+    assert _err(f1, f0) <= tol * 10
+    assert np.array_equal(ft1, ft0)
+
+
+@pytest.mark.parametrize("mode", [osolver.VEL_CURRENT, osolver.VEL_LAST_HALF])
+@pytest.mark.parametrize("prec,tol", [("double", TOL64), ("single", TOL32)])
+def test_coupled_fluid_solid_with_absorbers(bfe, coupled, mode, prec, tol):
+    m = coupled
+    nt = 500
+    t, s = modelgen.pulse(nt, m["dt"])
+    fi = modelgen.gi_of(m["gl"], [m["frc_nd"]], 4)          # pressure source in the water
+    hi = np.concatenate([modelgen.gi_of(m["gl"], m["mon_nds"], 4),
+                         modelgen.gi_of(m["gl"], m["mon_nds"], 2)])
+    h0, _, _, _ = _oracle(m, t, fi, s, hi, mode=mode)
+    h1, _, _, _ = bfe.fn_explicit_dynamic_solver_gb300(
+        m["K"], m["C"], m["M"], t, fi, s, [], [], hi, np.inf, 1, "KE", mode, prec, gl_lookup=m["gl"])
+    assert np.isfinite(h0).all()
+    # fluid (pressure) and solid (displacement) rows have different units:
+    # normalise each family separately
+    q4 = modelgen.gi_of(m["gl"], m["mon_nds"], 4).size
+    assert _err(h1[:q4], h0[:q4]) <= tol
+    assert _err(h1[q4:], h0[q4:]) <= tol
+
+
+@pytest.mark.parametrize("prec,tol", [("double", TOL64), ("single", TOL32)])
+def test_forcing_rows_duplicates_and_start(bfe, plate, prec, tol):
+    m = plate
+    nt = 300
+    t, s = modelgen.pulse(nt, m["dt"])
+    s = np.concatenate([np.zeros(37), s[:-37]])             # ti_start = 38 (1-based)
+    nds = [m["frc_nd"], m["frc_nd"] - 1, m["frc_nd"] + 1, m["frc_nd"]]
+    fi = modelgen.gi_of(m["gl"], nds, 2)                     # duplicate DOF: last row wins
+    F = np.vstack([s, 0.5 * s, -0.25 * s, 2.0 * s])
+    hi = np.concatenate([fi, modelgen.gi_of(m["gl"], m["mon_nds"], 1)])
+    h0, _, _, _ = _oracle(m, t, fi, F, hi)
+    h1, _, _, _ = bfe.fn_explicit_dynamic_solver_gb300(
+        m["K"], m["C"], m["M"], t, fi, F, [], [], hi, np.inf, 1, "KE", osolver.VEL_CURRENT, prec,
+        gl_lookup=m["gl"])
+    assert np.all(h1[:, :37] == 0)
+    assert _err(h1, h0) <= tol
+
+
+def test_zero_forcing_runs_no_steps(bfe, plate):
+    m = plate
+    t = np.arange(50) * m["dt"]
+    fi = modelgen.gi_of(m["gl"], [m["frc_nd"]], 2)
+    h1, f1, _, ft = bfe.fn_explicit_dynamic_solver_gb300(
+        m["K"], m["C"], m["M"], t, fi, np.zeros(50), [], [], fi, 10, 1, "KE", osolver.VEL_CURRENT, "double")
+    assert np.all(h1 == 0) and np.all(f1 == 0) and np.all(ft == 0)
+
+
+def test_displacement_field_output(bfe, plate):
+    m = plate
+    nt = 200
+    t, s = modelgen.pulse(nt, m["dt"])
+    fi = modelgen.gi_of(m["gl"], [m["frc_nd"]], 2)
+    h0, f0, _, ft0 = _oracle(m, t, fi, s, fi, every=33, ftype="mean(u2)")
+    h1, f1, _, ft1 = bfe.fn_explicit_dynamic_solver_gb300(
+        m["K"], m["C"], m["M"], t, fi, s, [], [], fi, 33, 1, "mean(u2)", osolver.VEL_CURRENT, "double")
+    assert _err(f1, f0) <= TOL64 and np.array_equal(ft0, ft1)
+
+
+@pytest.mark.parametrize("prec", ["double", "single"])
+def test_batched_sources_equal_single_runs(bfe, coupled, prec):
+    m = coupled
+    nt = 300
+    t, s = modelgen.pulse(nt, m["dt"])
+    top = m["mon_nds"][:4]
+    srcs = [modelgen.gi_of(m["gl"], [nd], 4) for nd in top]
+    hi = np.concatenate([modelgen.gi_of(m["gl"], m["mon_nds"], 4),
+                         modelgen.gi_of(m["gl"], m["mon_nds"], 2)])
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, prec, m["gl"]) as plan:
+        hb = plan.run_batched(t, srcs, s, hi)
+        for r, fi in enumerate(srcs):
+            h1, _, _ = plan.run(t, fi, s, hi)
+            assert np.abs(hb[:, :, r] - h1).max() <= 1e-12 * max(np.abs(h1).max(), 1e-300)
+    # and against the oracle for one source
+    h0, _, _, _ = _oracle(m, t, srcs[1], s, hi)
+    q4 = modelgen.gi_of(m["gl"], m["mon_nds"], 4).size
+    tol = TOL64 if prec == "double" else TOL32
+    assert _err(hb[:q4, :, 1], h0[:q4]) <= tol
+
+
+def test_batched_64_sources_fp32(bfe, coupled):
+    m = coupled
+    nt = 200
+    t, s = modelgen.pulse(nt, m["dt"])
+    nds = np.nonzero(m["gl"][:, 3] > 0)[0] + 1
+    srcs = [modelgen.gi_of(m["gl"], [nds[(7 * r) % nds.size]], 4) for r in range(64)]
+    hi = modelgen.gi_of(m["gl"], m["mon_nds"], 4)
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, "single", m["gl"]) as plan:
+        hb = plan.run_batched(t, srcs, s, hi)
+    for r in (0, 17, 63):
+        h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
+        assert _err(hb[:, :, r], h0) <= TOL32
+
+
+def test_errors_through_the_abi(bfe, plate):
+    m = plate
+    t = np.arange(20) * m["dt"]
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"]) as plan:
+        with pytest.raises(bfe.BfeError) as ei:
+            plan.run(t, [m["K"].shape[0] + 5], np.ones(20), [1])
+        assert ei.value.status == 1
+        with pytest.raises(bfe.BfeError):
+            plan.run(t * 2, [1], np.ones(20), [1])                 # dt mismatch
+        with pytest.raises(bfe.BfeError):
+            plan.run(t, [1, 2], np.ones((3, 20)), [1])             # 3 rows for 2 DOFs
