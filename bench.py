@@ -1,0 +1,403 @@
+"""Benchmark of the explicit time-marching path on one GB300 (or N replicas).
+
+Headline: FP32 batched time marching (64 sources as 64 right-hand sides of one
+launch sequence) on the coupled water/steel model - 60 x 30 mm at 0.05 mm
+(1.44M triangles), ASI2D2 interface, quadratic absorbing layers, seeded void
+blob, 64-element array on the water surface - over 6,000 samples. One bench
+step = one full march of all sources. Also measured in the same run: the
+plain FP64 form on the same model (one source), the max-normalised A-scan
+error of the FP32 batched result against that FP64 run, the step kernel's
+roofline, the end-to-end call through the C ABI with host buffers, and the
+FP64 CPU restatement of the reference's time loop on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "bristolfe-v2_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "DOF-updates/s & HBM GB/s: FP32 batched vs plain FP64 GPU at ≤1e-4 A-scan err"
+UNIT = "DOF-updates/s"
+
+WORKLOAD = dict(W=60e-3, H_water=20e-3, H_steel=10e-3, h=0.05e-3, fc=5e6, cycles=5,
+                n_t=6000, n_src=64, pitch=0.6e-3, blob_radius=1.5e-3, seed=0)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="shrink the model size (testing only; 1.0 = the benchmark model)")
+    ap.add_argument("--n-t", type=int, default=None)
+    return ap.parse_args()
+
+
+def blob_polygon(radius, centre, seed, n_harm=8, amp_max=0.2, n_pts=128):
+    """Seeded smooth random void: r(a) = R (1 + sum_k A_k sin(k a + phi_k)) /
+    (1 + sum A_k / 2), A_k ~ U(0, amp_max), k = 1..n_harm."""
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(0.0, amp_max, n_harm)
+    phi = rng.uniform(0.0, 2 * np.pi, n_harm)
+    a = np.linspace(0, 2 * np.pi, n_pts, endpoint=False)
+    k = np.arange(1, n_harm + 1)
+    r = radius * (1 + (A[None, :] * np.sin(a[:, None] * k[None, :] + phi[None, :])).sum(1)) / (1 + A.sum() / 2)
+    return np.column_stack([r * np.cos(a), r * np.sin(a)]) + np.asarray(centre)
+
+
+def workload(scale):
+    w = dict(WORKLOAD)
+    if scale != 1.0:
+        w["W"] *= scale
+        w["H_water"] *= scale
+        w["H_steel"] *= scale
+        w["pitch"] *= scale
+        w["blob_radius"] *= scale
+    w["blob"] = blob_polygon(w["blob_radius"], (w["W"] / 2, w["H_steel"] / 2), w["seed"])
+    return w
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle-reason sampling during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(nnz, n, R, p, q, b):
+    """Bytes one time step must move (per launch of the step kernel):
+    operator values + int32 columns, row pointers, two per-row coefficient
+    vectors, read u_n, read u_{n-1}, write u_{n+1} per RHS, forcing and
+    monitor values."""
+    return nnz * (b + 4) + 4 * (n + 1) + 2 * n * b + 3 * R * n * b + R * (p + q) * b
+
+
+def run_ours(args):
+    import torch
+    import bfe_gb300
+    from bfe_gb300 import model
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    bfe_gb300.load()
+    w = workload(args.scale)
+    n_t = args.n_t or w["n_t"]
+    t0 = time.perf_counter()
+    m = model.coupled_water_steel(W=w["W"], H_water=w["H_water"], H_steel=w["H_steel"], h=w["h"],
+                                  fc=w["fc"], blob_polygon_pts=w["blob"],
+                                  array_elements=w["n_src"], array_pitch=w["pitch"])
+    t_build = time.perf_counter() - t0
+    K, C, M, gl, dt = m["K"], m["C"], m["M"], m["gl"], m["dt"]
+    n = K.shape[0]
+    t = np.arange(n_t) * dt
+    sig = model.toneburst(t, w["fc"], w["cycles"])
+    srcs = [model.global_indices(gl, nodes, 4) for nodes in m["src_nodes"]]
+    mons = model.global_indices(gl, m["mon_nodes"], 4)
+    R, q = len(srcs), mons.size
+    p_max = max(s.size for s in srcs)
+    t0 = time.perf_counter()
+    plan32 = bfe_gb300.Plan(K, C, M, dt, bfe_gb300.VEL_CURRENT, "single", gl)
+    plan64 = bfe_gb300.Plan(K, C, M, dt, bfe_gb300.VEL_CURRENT, "double", gl)
+    t_plan = time.perf_counter() - t0
+
+    # device-resident inputs: one shared signal, forcing map, zeroed history
+    frc_dof = np.concatenate([s - 1 for s in srcs])
+    frc_rhs = np.concatenate([np.full(s.size, r) for r, s in enumerate(srcs)])
+    frc_sig = np.zeros(frc_dof.size, np.int64)
+    d_sig = torch.tensor(sig, dtype=torch.float64, device="cuda").reshape(n_t, 1)
+    d_hist = torch.zeros((R, n_t, q), dtype=torch.float64, device="cuda")
+    nz = np.nonzero(sig)[0]
+    ti0 = int(nz.min())
+    steps_per_march = n_t - ti0
+    stream = torch.cuda.current_stream()
+
+    def march32():
+        d_hist.zero_()
+        plan32.run_device(R, n_t, ti0, frc_dof, frc_rhs, frc_sig, None, d_sig, mons - 1, d_hist,
+                          stream.cuda_stream)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        march32()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            march32()
+        ev1.record(stream)
+        barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    if dist is not None:
+        tt = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_total = float(tt.item())
+    ms_step = ms_total / args.steps
+    st32 = plan32.stats()
+    launches = args.steps * (st32["step_launches"] + st32["aux_launches"])
+    value = world * R * n * steps_per_march / (ms_step * 1e-3)
+    h32 = d_hist.cpu().numpy()                                # (R, n_t, q)
+
+    # per-kernel timing pass (CUDA events around every launch, same stream)
+    plan32.set_timing(True)
+    march32()
+    torch.cuda.synchronize()
+    stk = plan32.stats()
+    plan32.set_timing(False)
+    step_avg_ms = stk["step_ms"] / max(stk["step_launches"], 1)
+    nnz = K.nnz
+    bytes_step = algorithmic_bytes(nnz, n, R, p_max, q, 4)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = bytes_step / (step_avg_ms * 1e-3) / 1e9
+
+    # plain FP64 form on the same model, one source (the middle element)
+    r_mid = R // 2
+    sel = frc_rhs == r_mid
+    d_hist64 = torch.zeros((1, n_t, q), dtype=torch.float64, device="cuda")
+
+    def march64():
+        d_hist64.zero_()
+        plan64.run_device(1, n_t, ti0, frc_dof[sel], np.zeros(sel.sum(), np.int64),
+                          frc_sig[sel], None, d_sig, mons - 1, d_hist64, stream.cuda_stream)
+    march64()
+    torch.cuda.synchronize()
+    k64 = 2
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k64):
+        march64()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / k64
+    value64 = n * steps_per_march / (ms64 * 1e-3)
+    plan64.set_timing(True)
+    march64()
+    torch.cuda.synchronize()
+    st64 = plan64.stats()
+    plan64.set_timing(False)
+    step64_ms = st64["step_ms"] / max(st64["step_launches"], 1)
+    bytes64 = algorithmic_bytes(nnz, n, 1, srcs[r_mid].size, q, 8)
+    h64 = d_hist64.cpu().numpy()[0]
+    err = float(np.abs(h32[r_mid] - h64).max() / np.abs(h64).max())
+
+    # end to end through the C ABI with host buffers (H2D signals, D2H A-scans)
+    e2e_steps = max(1, min(args.steps, 3))
+    th0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        hist_host = plan32.run_batched(t, [s for s in srcs], sig, mons)
+    e2e_s = (time.perf_counter() - th0) / e2e_steps
+    e2e_value = world * R * n * steps_per_march / e2e_s
+    h2d = 8 * n_t * R + 8 * (p_max * R + q)          # signals (repeated per source) + indices
+    d2h = 8 * q * n_t * R
+
+    result = None
+    if rank == 0:
+        cpu = cpu_baseline(K, C, M, dt, t, srcs[r_mid], sig, mons) if world == 1 else None
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "coupled water/steel 60x30 mm at 0.05 mm (1.44M triangles, "
+                                   "ASI2D2 interface, quadratic absorbers, void blob), 64-source "
+                                   "array FMC as 64 RHS, %d samples, FP32 batched" % n_t,
+                       "n_dof": n, "nnz_K": int(nnz), "sources": R, "monitors": q,
+                       "samples": n_t, "steps_marched_per_source": steps_per_march,
+                       "l2": "inputs larger than L2 (state %.0f MB per time step)" % (3 * R * n * 4 / 1e6),
+                       "parallelism": "replicas x%d" % world, "scale": args.scale},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "step_batched<float,2>", "bytes_per_launch": bytes_step,
+                         "avg_launch_ms": step_avg_ms, "peak_source": peak_kind},
+            "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_march": ms64,
+                           "step_kernel_ms": step64_ms,
+                           "step_kernel_gbs": bytes64 / (step64_ms * 1e-3) / 1e9,
+                           "speedup_fp32_batched": value / world / value64},
+            "ascan_err_vs_fp64": err,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+            "setup_s": {"model_build": t_build, "plans": t_plan},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(result), flush=True)
+    plan32.close()
+    plan64.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return result
+
+
+def cpu_baseline(K, C, M, dt, t, src_gi, sig, mons, target_s=10.0):
+    """The FP64 CPU restatement of the reference's time loop (oracle port) on
+    all host threads, timed on a bounded prefix of one source's march."""
+    from oracle import cpu_port
+    op = cpu_port.CpuOperator(K, C, M, dt)
+    n = K.shape[0]
+    probe = 20
+    _, s = cpu_port.time_march(op, t[:probe], src_gi - 1, sig[None, :probe], mons - 1)
+    steps = int(min(len(t), max(probe, target_s / max(s / probe, 1e-9))))
+    _, s = cpu_port.time_march(op, t[:steps], src_gi - 1, sig[None, :steps], mons - 1)
+    return {"value": n * steps / s, "unit": UNIT, "cores": cpu_port.threads(), "kind": "port",
+            "sample": "one source, first %d of %d samples, FP64 v6 loop (C, OpenMP)" % (steps, len(t))}
+
+
+def run_reference(args):
+    """The reference's CPU path (FP64 oracle port of the v6 loop on all host
+    threads) on the same workload, each step a bounded sample."""
+    rank = int(os.environ.get("RANK", 0))
+    if rank != 0:
+        return None
+    from oracle import assembly, cpu_port, mesh, signals
+    w = workload(args.scale)
+    n_t = args.n_t or w["n_t"]
+    steel = dict(rho=8000.0, D=signals.isotropic_stiffness_matrix(210e9, 0.3), el_typ="CPE3")
+    water = dict(rho=1000.0, D=1500.0 ** 2 * 1000.0, el_typ="AC2D3")
+    matls = [steel, water]
+    Ht = w["H_water"] + w["H_steel"]
+    mod = mesh.rectangular_structured_mesh(np.array([[0, 0], [w["W"], 0], [w["W"], Ht], [0, Ht]]), w["h"])
+    mod = mesh.set_els_inside_bdry_to_mat(
+        mod, np.array([[-1, w["H_steel"]], [w["W"] + 1, w["H_steel"]], [w["W"] + 1, Ht + 1], [-1, Ht + 1]]), 2)
+    mod = mesh.remove_elements_in_region(mod, w["blob"])
+    mod["el_typ_i"] = [matls[k - 1]["el_typ"] for k in mod["el_mat_i"]]
+    cL = np.sqrt(steel["D"][0, 0] / steel["rho"])
+    th = 3.0 * cL / w["fc"]
+    inner = np.array([[th, th], [w["W"] - th, th], [w["W"] - th, Ht + 1.0], [th, Ht + 1.0]])
+    mod = mesh.add_absorbing_layer(mod, inner, th)
+    mod = mesh.add_fluid_solid_interface_els(mod, matls)
+    K, C, M, gl = assembly.build_global_matrices_v5(mod["nds"], mod["els"], mod["el_mat_i"], mod["el_abs_i"],
+                                                    mod["el_typ_i"], matls,
+                                                    dict(dof_to_use=[1, 2, 4], damping_power_law=2))
+    solid = np.array([x == "CPE3" for x in mod["el_typ_i"]])
+    dt = signals.element_eigen_time_step(mod["nds"], mod["els"][solid, :3], steel["D"], steel["rho"])
+    t = np.arange(n_t) * dt
+    sig = signals.gaussian_pulse(t, w["fc"], w["cycles"])
+    top = np.nonzero(np.isclose(mod["nds"][:, 1], Ht))[0]
+    xc = w["W"] / 2 + (np.arange(w["n_src"]) - (w["n_src"] - 1) / 2) * w["pitch"]
+    mid = top[np.abs(mod["nds"][top, 0] - xc[w["n_src"] // 2]) <= 0.4 * w["pitch"] + 1e-12] + 1
+    src = gl[mid - 1, 3]
+    src = src[src > 0]
+    mons = np.array([gl[top[np.argmin(np.abs(mod["nds"][top, 0] - x))], 3] for x in xc])
+    op = cpu_port.CpuOperator(K, C, M, dt)
+    n = K.shape[0]
+    probe = 10
+    _, s = cpu_port.time_march(op, t[:probe], src - 1, sig[None, :probe], mons - 1)
+    per = max(s / probe, 1e-9)
+    steps = int(min(n_t, max(probe, 8.0 / per)))
+    for _ in range(args.warmup):
+        cpu_port.time_march(op, t[:steps], src - 1, sig[None, :steps], mons - 1)
+    secs = []
+    for _ in range(args.steps):
+        _, s = cpu_port.time_march(op, t[:steps], src - 1, sig[None, :steps], mons - 1)
+        secs.append(s)
+    s = sum(secs) / len(secs)
+    value = n * steps / s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": int(os.environ.get("WORLD_SIZE", 1)), "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "coupled water/steel 60x30 mm at 0.05 mm, reference CPU v6 loop "
+                               "(FP64), one source per bounded sample", "n_dof": n, "samples": n_t,
+                   "sample_steps": steps, "scale": args.scale},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_port.threads(), "kind": "port",
+                         "sample": "first %d of %d samples of one source" % (steps, n_t)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

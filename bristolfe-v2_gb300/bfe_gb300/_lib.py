@@ -39,6 +39,12 @@ class BfeSparse(ctypes.Structure):
                 ("ptr", PI64), ("idx", PI64), ("val", PD)]
 
 
+class BfeStats(ctypes.Structure):
+    _fields_ = [("step_launches", I64), ("aux_launches", I64), ("step_ms", ctypes.c_double),
+                ("aux_ms", ctypes.c_double), ("n_dof", I64), ("nnz_stored", I64),
+                ("nnz_padded", I64), ("n_interface", I64), ("n_direct_rows", I64)]
+
+
 SIGNATURES = {
     "bfe_plan_create": (I32, [ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
                               ctypes.POINTER(BfeSparse), ctypes.c_double, I32, I32,
@@ -49,6 +55,8 @@ SIGNATURES = {
     "bfe_run_batched": (I32, [VP, I64, I64, PD, I64, PI64, I64, PD, I64, PI64, PD]),
     "bfe_run_device": (I32, [VP, I64, I64, I64, I64, PI64, PI64, PI64, PD, I64, VP,
                              I64, PI64, VP, VP]),
+    "bfe_plan_set_timing": (I32, [VP, I32]),
+    "bfe_plan_stats": (I32, [VP, ctypes.POINTER(BfeStats)]),
     "bfe_last_error": (ctypes.c_char_p, []),
     "bfe_version": (I32, [PI32, PI32, PI32]),
 }

@@ -1,0 +1,388 @@
+"""Synthetic model generation and global assembly (host, vectorised NumPy).
+
+These are the model-preparation utilities a user of the solver runs before
+the time march: structured triangle meshes, material regions, fluid-solid
+interface elements, absorbing layers, void scatterers, and the v5 global
+assembly with the reference's DOF numbering. They follow
+
+    code/fn_rectangular_structured_mesh.m:14-57 (mesh, node/element order)
+    code/fn_set_els_inside_bdry_to_mat.m, code/fn_elements_in_region.m
+    code/fn_add_fluid_solid_interface_els.m:26-73 (ASI2D2 insertion)
+    code/fn_add_absorbing_layer.m:1-17 (absorbing index)
+    code/fn_add_scatterer.m:16-20 (void scatterer)
+    code/internal/fn_build_global_matrices_v5.m:50-159 (assembly, numbering)
+    code/internal/elements/el_builder/el_sym_{CPE3,AC2D3,ASI2D2}.m (elements)
+
+Everything here is vectorised over elements (no per-element Python loops),
+so the 1.44M-element benchmark model assembles in seconds. Indices in the
+returned model are 1-based like the reference's; gl_lookup holds 1-based
+global indices (0 = no DOF).
+"""
+import numpy as np
+import scipy.sparse as sp
+
+TYPE_CODES = {"CPE3": 0, "AC2D3": 1, "ASI2D2": 2}
+TYPE_DOFS = {"CPE3": (1, 2, 3), "AC2D3": (4,), "ASI2D2": (1, 2, 3, 4)}
+
+
+def isotropic_stiffness(E, nu):
+    """6x6 isotropic stiffness, engineering shear (fn_isotropic_stiffness_matrix.m:17-23)."""
+    lam = E / (1 - 2 * nu) / (1 + nu)
+    D = np.zeros((6, 6))
+    D[:3, :3] = lam * nu
+    D[[0, 1, 2], [0, 1, 2]] = lam * (1 - nu)
+    D[[3, 4, 5], [3, 4, 5]] = lam * (1 - 2 * nu) / 2
+    return D
+
+
+def toneburst(t, fc, cycles):
+    """-40 dB Gaussian toneburst starting at its 1% envelope point (fn_gaussian_pulse.m:1-15)."""
+    t = np.asarray(t, float)
+    ct = t.mean()
+    T = cycles / (2 * fc * np.sqrt(np.log(100.0)))
+    env = np.exp(-((t - ct) / T) ** 2)
+    first = int(np.argmax(env > 0.01))
+    s = env * np.sin(2 * np.pi * fc * (t - ct))
+    return np.concatenate([s[first:], np.zeros(first)])
+
+
+def rect_mesh(x0, x1, y0, y1, h):
+    """Right-isosceles structured mesh with the reference's node and element
+    order (column-major node numbering, 'a' triangles then 'b' triangles)."""
+    nx = int(np.ceil(abs(x1 - x0) / h)) + 1
+    ny = int(np.ceil(abs(y1 - y0) / h)) + 1
+    x = np.linspace(x0, x1, nx)
+    y = np.linspace(y0, y1, ny)
+    nds = np.column_stack([np.repeat(x, ny), np.tile(y, nx)])        # node k = r + c*ny
+    r, c = np.meshgrid(np.arange(ny - 1), np.arange(nx - 1), indexing="ij")
+    r = r.ravel(order="F")
+    c = c.ravel(order="F")
+    n00 = r + c * ny + 1
+    n10 = (r + 1) + c * ny + 1
+    n01 = r + (c + 1) * ny + 1
+    n11 = (r + 1) + (c + 1) * ny + 1
+    els = np.vstack([np.column_stack([n00, n11, n10]), np.column_stack([n00, n01, n11])])
+    return nds, els.astype(np.int64)
+
+
+def centroids(nds, els):
+    m = (els > 0).sum(1, keepdims=True)
+    idx = np.where(els > 0, els, 1) - 1
+    return (nds[idx] * (els > 0)[:, :, None]).sum(1) / m
+
+
+def points_in_polygon(pts, poly):
+    """Crossing-number test (boundary points count as inside, like inpolygon)."""
+    x, y = pts[:, 0], pts[:, 1]
+    inside = np.zeros(x.shape, bool)
+    on = np.zeros(x.shape, bool)
+    P = np.asarray(poly, float)
+    Q = np.roll(P, -1, axis=0)
+    scale = max(np.ptp(P[:, 0]), np.ptp(P[:, 1]), 1e-300)
+    for (xa, ya), (xb, yb) in zip(P, Q):
+        crosses = (ya > y) != (yb > y)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            xi = xa + (y - ya) * (xb - xa) / (yb - ya)
+        inside ^= crosses & (x < xi)
+        dx, dy = xb - xa, yb - ya
+        L2 = dx * dx + dy * dy
+        if L2 > 0:
+            t = ((x - xa) * dx + (y - ya) * dy) / L2
+            d = np.hypot(x - (xa + t * dx), y - (ya + t * dy))
+            on |= (t >= -1e-12) & (t <= 1 + 1e-12) & (d <= 1e-12 * scale)
+    return inside | on
+
+
+def distance_to_polygon(pts, poly):
+    """Distance to the nearest polygon vertex or to one of its two adjacent
+    edges (fn_dist_point_to_bdry_2D.m:1-69 restricted to that vertex)."""
+    P = np.asarray(poly, float)
+    nb = P.shape[0]
+    d2 = ((pts[:, None, :] - P[None, :, :]) ** 2).sum(-1)
+    j = np.argmin(d2, axis=1)
+    best = np.sqrt(d2[np.arange(pts.shape[0]), j])
+    for step in (1, -1):
+        a = P[j]
+        b = P[(j + step) % nb]
+        ab = b - a
+        L = np.sqrt((ab ** 2).sum(1))
+        u = ab / L[:, None]
+        s = ((pts - a) * u).sum(1)
+        perp = np.sqrt((((pts - a) - s[:, None] * u) ** 2).sum(1))
+        s = s / L
+        best = np.minimum(best, np.where((s < 0) | (s > 1), np.inf, perp))
+    return best
+
+
+def remove_unused_nodes(nds, els):
+    used = np.unique(els[els > 0])
+    remap = np.zeros(nds.shape[0] + 1, np.int64)
+    remap[used] = np.arange(1, used.size + 1)
+    return nds[used - 1], remap[els]
+
+
+def fluid_solid_interfaces(nds, els, typ):
+    """ASI2D2 elements on every edge shared by an AC2D3 and a CPE3 element,
+    node order chosen so the fluid centroid lies on the side of
+    [a_y, -a_x], a = x2 - x1 (fn_add_fluid_solid_interface_els.m:175-195).
+    Returns the (n_int, 2) 1-based node pairs in sorted-edge order."""
+    tri = np.nonzero(typ != TYPE_CODES["ASI2D2"])[0]
+    E = els[tri, :3]
+    edges = np.vstack([E[:, [0, 1]], E[:, [1, 2]], E[:, [2, 0]]])
+    owner = np.concatenate([tri, tri, tri])
+    key_e = np.sort(edges, axis=1)
+    key = key_e[:, 0] * (nds.shape[0] + 1) + key_e[:, 1]
+    order = np.argsort(key, kind="stable")
+    key, owner, key_e = key[order], owner[order], key_e[order]
+    same = key[1:] == key[:-1]
+    a_el, b_el = owner[:-1][same], owner[1:][same]
+    ta, tb = typ[a_el], typ[b_el]
+    fl, so = TYPE_CODES["AC2D3"], TYPE_CODES["CPE3"]
+    mix = ((ta == fl) & (tb == so)) | ((ta == so) & (tb == fl))
+    ed = key_e[:-1][same][mix].copy()
+    fluid_el = np.where(ta[mix] == fl, a_el[mix], b_el[mix])
+    ctr = centroids(nds, els[fluid_el])
+    a = nds[ed[:, 1] - 1] - nds[ed[:, 0] - 1]
+    b = np.column_stack([a[:, 1], -a[:, 0]])
+    c = ctr - nds[ed[:, 0] - 1]
+    flip = (c * b).sum(1) < 0
+    ed[flip] = ed[flip][:, ::-1]
+    return ed
+
+
+# ---------------------------------------------------------------------------
+# Element matrices (vectorised). Each returns (K, C, M, loc_nd, loc_df) with
+# matrices (n_el, ndf, ndf) restricted to the requested DOFs.
+
+def _tri_grads(nds, e):
+    x = nds[e[:, :3] - 1, 0]
+    y = nds[e[:, :3] - 1, 1]
+    J = (x[:, 0] - x[:, 2]) * (y[:, 1] - y[:, 2]) - (x[:, 1] - x[:, 2]) * (y[:, 0] - y[:, 2])
+    gx = np.column_stack([y[:, 1] - y[:, 2], y[:, 2] - y[:, 0], y[:, 0] - y[:, 1]]) / J[:, None]
+    gy = np.column_stack([x[:, 2] - x[:, 1], x[:, 0] - x[:, 2], x[:, 1] - x[:, 0]]) / J[:, None]
+    return J, gx, gy
+
+
+def _select(dofs_all, nodes_all, keep):
+    sel = np.nonzero(np.isin(dofs_all, keep))[0]
+    return sel, nodes_all[sel], dofs_all[sel]
+
+
+def cpe3(nds, e, D, rho, keep):
+    J, gx, gy = _tri_grads(nds, e)
+    n = e.shape[0]
+    # strain rows [e11, e22, e33, g23, g13, g12]; local dof order (node, dof 1..3)
+    B = np.zeros((n, 6, 9))
+    for a in range(3):
+        B[:, 0, 3 * a] = gx[:, a]
+        B[:, 1, 3 * a + 1] = gy[:, a]
+        B[:, 3, 3 * a + 2] = gy[:, a]
+        B[:, 4, 3 * a + 2] = gx[:, a]
+        B[:, 5, 3 * a] = gy[:, a]
+        B[:, 5, 3 * a + 1] = gx[:, a]
+    sel, ln, ld = _select(np.tile([1, 2, 3], 3), np.repeat([1, 2, 3], 3), keep)
+    Bs = B[:, :, sel]
+    K = np.matmul(np.matmul(Bs.transpose(0, 2, 1), D), Bs) * (0.5 * J)[:, None, None]
+    M = np.zeros_like(K)
+    ii = np.arange(sel.size)
+    M[:, ii, ii] = (rho * J / 6.0)[:, None]
+    return K, np.zeros_like(K), M, ln, ld
+
+
+def ac2d3(nds, e, bulk, rho, keep):
+    J, gx, gy = _tri_grads(nds, e)
+    sel, ln, ld = _select(np.array([4, 4, 4]), np.array([1, 2, 3]), keep)
+    G = gx[:, :, None] * gx[:, None, :] + gy[:, :, None] * gy[:, None, :]
+    K = (-0.5 / rho) * G * J[:, None, None]
+    M = np.zeros_like(K)
+    ii = np.arange(3)
+    M[:, ii, ii] = (-J / (6.0 * bulk))[:, None]
+    return K[:, sel][:, :, sel], np.zeros((e.shape[0], sel.size, sel.size)), M[:, sel][:, :, sel], ln, ld
+
+
+def asi2d2(nds, e, keep):
+    p1 = nds[e[:, 0] - 1]
+    p2 = nds[e[:, 1] - 1]
+    d = p1 - p2
+    # -L/4 * unit normal [d_y, -d_x]/L  =  [-d_y, d_x] / 4
+    cx = -d[:, 1] / 4.0
+    cy = d[:, 0] / 4.0
+    n = e.shape[0]
+    C = np.zeros((n, 8, 8))
+    for s in (0, 4):
+        for f in (3, 7):
+            C[:, s, f] = C[:, f, s] = cx
+            C[:, s + 1, f] = C[:, f, s + 1] = cy
+    sel, ln, ld = _select(np.tile([1, 2, 3, 4], 2), np.repeat([1, 2], 4), keep)
+    Cs = C[:, sel][:, :, sel]
+    return np.zeros_like(Cs), Cs, np.zeros_like(Cs), ln, ld
+
+
+def assemble(nds, els, el_mat, el_abs, typ, matls, dof_to_use=None, damping_power_law=3,
+             max_damping=3.1415e7, max_stiffness_reduction=0.01):
+    """Global K, C, M (CSR over the reduced DOFs) and gl_lookup.
+
+    typ holds TYPE_CODES per element; matls is a list of dicts with 'D' (6x6
+    or scalar bulk modulus) and 'rho'. Numbering: gi = (node-1)*max_df + dof,
+    then DOFs with empty K, M and C columns are removed
+    (fn_build_global_matrices_v5.m:127-159, fn_reduce_global_matrices.m:7-22)."""
+    names = {v: k for k, v in TYPE_CODES.items()}
+    present = sorted({names[c] for c in np.unique(typ)})
+    keep = list(dof_to_use) if dof_to_use else None
+    dofs_in_use = set()
+    for t in present:
+        d = np.array(TYPE_DOFS[t])
+        dofs_in_use |= set(d[np.isin(d, keep)] if keep else d)
+    max_df = max(dofs_in_use)
+    n_nodes = nds.shape[0]
+    rows, cols, kv, cv, mv = [], [], [], [], []
+    for t in present:
+        tsel = typ == TYPE_CODES[t]
+        for mat in np.unique(el_mat[tsel]):
+            es = np.nonzero(tsel & (el_mat == mat))[0]
+            e = els[es]
+            kd = keep if keep else list(TYPE_DOFS[t])
+            if t == "CPE3":
+                mt = matls[mat - 1]
+                K, C, M, ln, ld = cpe3(nds, e, np.asarray(mt["D"], float), mt["rho"], kd)
+            elif t == "AC2D3":
+                mt = matls[mat - 1]
+                K, C, M, ln, ld = ac2d3(nds, e, float(mt["D"]), mt["rho"], kd)
+            else:
+                K, C, M, ln, ld = asi2d2(nds, e, kd)
+            a = el_abs[es][:, None, None]
+            C = C + M * a ** damping_power_law * max_damping
+            K = K * np.exp(np.log(max_stiffness_reduction) * a ** (damping_power_law + 1))
+            g = (e[:, ln - 1] - 1) * max_df + (ld - 1)                 # (n_el, ndf) 0-based
+            ndf = ld.size
+            rows.append(np.repeat(g, ndf, axis=1).ravel())             # K(g_c, g_r) += el(r, c)
+            cols.append(np.tile(g, (1, ndf)).ravel())
+            kv.append(K.transpose(0, 2, 1).ravel())
+            cv.append(C.transpose(0, 2, 1).ravel())
+            mv.append(M.transpose(0, 2, 1).ravel())
+    N = n_nodes * max_df
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+
+    def build(vals):
+        A = sp.csr_matrix((np.concatenate(vals), (r, c)), shape=(N, N))
+        A.sum_duplicates()
+        A.eliminate_zeros()
+        return A
+
+    K, C, M = build(kv), build(cv), build(mv)
+    used = (np.asarray(abs(K).sum(0)).ravel() > 0) | (np.asarray(abs(M).sum(0)).ravel() > 0) | \
+        (np.asarray(abs(C).sum(0)).ravel() > 0)
+    keep_idx = np.nonzero(used)[0]
+    K = K[keep_idx][:, keep_idx].tocsr()
+    C = C[keep_idx][:, keep_idx].tocsr()
+    M = M[keep_idx][:, keep_idx].tocsr()
+    gl = np.zeros((n_nodes, max_df), np.int64)
+    gl[keep_idx // max_df, keep_idx % max_df] = np.arange(1, keep_idx.size + 1)
+    return K, C, M, gl
+
+
+def element_stable_dt(nds, els, D, rho, factor=0.9):
+    """factor * 2 / sqrt(max eigenvalue of M_e^-1 K_e) over CPE3 elements (in-plane)."""
+    K, _, M, _, _ = cpe3(nds, els, D, rho, [1, 2])
+    m = np.abs(np.einsum("eii->ei", M))
+    s = np.sign(np.einsum("eii->ei", M))
+    A = K * s[:, :, None] / np.sqrt(m[:, :, None] * m[:, None, :])
+    return factor * 2.0 / np.sqrt(np.linalg.eigvalsh(A).max())
+
+
+# ---------------------------------------------------------------------------
+# Benchmark model families
+
+STEEL = dict(rho=8000.0, E=210e9, nu=0.3)
+WATER = dict(rho=1000.0, c=1500.0)
+
+
+def steel_plate(W=20e-3, H=10e-3, h=0.1e-3, n_mon=16, dof_to_use=(1, 2)):
+    """Plain FP64 2D solid workload: rectangular mesh, point force at the
+    top-surface centre node (DOF 2), n_mon top-surface monitors."""
+    nds, els = rect_mesh(0.0, W, 0.0, H, h)
+    D = isotropic_stiffness(STEEL["E"], STEEL["nu"])
+    matls = [dict(D=D, rho=STEEL["rho"])]
+    ne = els.shape[0]
+    typ = np.full(ne, TYPE_CODES["CPE3"])
+    K, C, M, gl = assemble(nds, els, np.ones(ne, np.int64), np.zeros(ne), typ, matls, dof_to_use)
+    dt = element_stable_dt(nds, els, D, STEEL["rho"])
+    top = np.nonzero(np.isclose(nds[:, 1], H))[0]
+    src = top[np.argmin(np.abs(nds[top, 0] - W / 2))]
+    mon = top[np.linspace(0, top.size - 1, n_mon).astype(int)]
+    return dict(nds=nds, els=els, typ=typ, K=K, C=C, M=M, gl=gl, dt=dt,
+                src_nodes=[src + 1], src_dof=2, mon_nodes=mon + 1, mon_dof=2)
+
+
+def smooth_blob(radius, n_harm, amp_max, rng, n_pts=128):
+    """Closed curve r(a) = radius * (1 + sum_k A_k sin(k a + phi_k)) / (1 + sum A_k),
+    A_k ~ U(0, amp_max), k = 1..n_harm (a seeded smooth random void)."""
+    A = rng.uniform(0.0, amp_max, n_harm)
+    phi = rng.uniform(0.0, 2 * np.pi, n_harm)
+    a = np.linspace(0, 2 * np.pi, n_pts, endpoint=False)
+    k = np.arange(1, n_harm + 1)
+    r = radius * (1 + (A[None, :] * np.sin(a[:, None] * k[None, :] + phi[None, :])).sum(1)) / (1 + A.sum() / 2)
+    return np.column_stack([r * np.cos(a), r * np.sin(a)])
+
+
+def coupled_water_steel(W=60e-3, H_water=20e-3, H_steel=10e-3, h=0.05e-3, fc=5e6,
+                        abs_wavelengths=3.0, blob_radius=1.5e-3, blob_centre=None,
+                        seed=0, dof_to_use=(1, 2, 4), damping_power_law=2,
+                        array_elements=64, array_pitch=0.6e-3, element_width=None,
+                        blob_polygon_pts=None):
+    """Coupled water-over-steel workload: ASI2D2 interface, absorbing layers
+    (left, right, bottom; thickness in steel longitudinal wavelengths,
+    quadratic grading), a void in the steel (the given polygon, or a seeded
+    smooth blob), and a linear array on the top (water) surface whose
+    elements are the sources/receivers."""
+    nds, els = rect_mesh(0.0, W, 0.0, H_water + H_steel, h)
+    D = isotropic_stiffness(STEEL["E"], STEEL["nu"])
+    bulk = WATER["c"] ** 2 * WATER["rho"]
+    matls = [dict(D=D, rho=STEEL["rho"]), dict(D=bulk, rho=WATER["rho"])]
+    ctr = centroids(nds, els)
+    el_mat = np.where(ctr[:, 1] > H_steel, 2, 1).astype(np.int64)
+    rng = np.random.default_rng(seed)
+    blob = None
+    if blob_polygon_pts is not None:
+        blob = np.asarray(blob_polygon_pts, float)
+    elif blob_radius > 0:
+        bc = np.array(blob_centre if blob_centre is not None else (W / 2, H_steel / 2))
+        blob = smooth_blob(blob_radius, 8, 0.2, rng) + bc
+    if blob is not None:
+        keep = ~points_in_polygon(ctr, blob)
+        els, el_mat = els[keep], el_mat[keep]
+        nds, els = remove_unused_nodes(nds, els)
+        ctr = centroids(nds, els)
+    cL = np.sqrt(D[0, 0] / STEEL["rho"])
+    thick = abs_wavelengths * cL / fc
+    Htot = H_water + H_steel
+    inner = np.array([[thick, thick], [W - thick, thick], [W - thick, Htot + 1.0], [thick, Htot + 1.0]])
+    el_abs = np.clip(distance_to_polygon(ctr, inner) / thick, 0.0, 1.0)
+    el_abs[points_in_polygon(ctr, inner)] = 0.0
+    typ = np.where(el_mat == 2, TYPE_CODES["AC2D3"], TYPE_CODES["CPE3"])
+    ed = fluid_solid_interfaces(nds, els, typ)
+    els_all = np.vstack([els, np.column_stack([ed, np.zeros(ed.shape[0], np.int64)])])
+    typ = np.concatenate([typ, np.full(ed.shape[0], TYPE_CODES["ASI2D2"])])
+    el_mat = np.concatenate([el_mat, np.zeros(ed.shape[0], np.int64)])
+    el_abs = np.concatenate([el_abs, np.zeros(ed.shape[0])])
+    K, C, M, gl = assemble(nds, els_all, el_mat, el_abs, typ, matls, dof_to_use,
+                           damping_power_law=damping_power_law)
+    solid = typ == TYPE_CODES["CPE3"]
+    dt = element_stable_dt(nds, els_all[solid, :3], D, STEEL["rho"])
+    # linear array on the top surface (water): element e covers
+    # [x_e - w/2, x_e + w/2] around x_e = W/2 + (e - (n-1)/2) * pitch
+    top = np.nonzero(np.isclose(nds[:, 1], Htot))[0]
+    width = element_width if element_width is not None else 0.8 * array_pitch
+    xc = W / 2 + (np.arange(array_elements) - (array_elements - 1) / 2) * array_pitch
+    src_nodes = [top[np.abs(nds[top, 0] - x) <= width / 2 + 1e-12] + 1 for x in xc]
+    centre_nodes = np.array([top[np.argmin(np.abs(nds[top, 0] - x))] + 1 for x in xc])
+    return dict(nds=nds, els=els_all, typ=typ, el_mat=el_mat, el_abs=el_abs, K=K, C=C, M=M,
+                gl=gl, dt=dt, src_nodes=src_nodes, src_dof=4, mon_nodes=centre_nodes,
+                mon_dof=4, matls=matls, n_interface=ed.shape[0])
+
+
+def global_indices(gl, nodes, dof):
+    """1-based global indices of (node, dof) pairs that exist (fn_BristolFE_v2.m:159-168)."""
+    g = gl[np.asarray(nodes, np.int64) - 1, dof - 1]
+    return g[g > 0]

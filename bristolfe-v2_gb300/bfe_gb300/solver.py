@@ -98,6 +98,16 @@ class Plan:
         check(lib.bfe_plan_ndof(self._h, ctypes.byref(nn)))
         self.n = nn.value
 
+    def set_timing(self, enable=True):
+        """CUDA-event timing of every launch in later runs (see stats())."""
+        check(self._lib.bfe_plan_set_timing(self._h, int(bool(enable))))
+
+    def stats(self):
+        """Counters of the last run as a dict (launches, device ms, nnz, ...)."""
+        st = _lib.BfeStats()
+        check(self._lib.bfe_plan_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.bfe_plan_destroy(self._h)

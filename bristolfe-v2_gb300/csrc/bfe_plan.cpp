@@ -227,7 +227,10 @@ struct bfe_plan {
   DevBuf<unsigned char> z_val;
   // statistics
   int64_t nnz_operator = 0;         // stored (unpadded) entries
+  int64_t nnz_padded = 0;
   int64_t n_direct_rows = 0;
+  bool timing = false;
+  bfe_stats last{};
 };
 
 namespace {
@@ -313,6 +316,18 @@ int bfe_version(int32_t* major, int32_t* minor, int32_t* patch) {
   if (major) *major = 0;
   if (minor) *minor = 1;
   if (patch) *patch = 0;
+  return BFE_OK;
+}
+
+int bfe_plan_set_timing(bfe_plan* plan, int32_t enable) {
+  if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
+  plan->timing = enable != 0;
+  return BFE_OK;
+}
+
+int bfe_plan_stats(const bfe_plan* plan, bfe_stats* out) {
+  if (!plan || !out) return fail(BFE_ERR_ARG, "NULL argument");
+  *out = plan->last;
   return BFE_OK;
 }
 
@@ -506,6 +521,7 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
     pl->max_slice_entries = std::max<int32_t>(pl->max_slice_entries, (int32_t)(w * bfe::kSlice));
   }
   pl->nnz_operator = stored;
+  pl->nnz_padded = (int64_t)hcol.size();
   pl->n_direct_rows = direct_rows;
   pl->h_acoef = acoef;
 
@@ -657,28 +673,71 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   a.v_int = d_vint.p;
   unsigned char* U[3] = {d_u.p, d_u.p + state_bytes, d_u.p + 2 * state_bytes};
   int iprev = 0, icur = 1, inew = 2;
+  bfe_stats& stt = pl->last;
+  stt = bfe_stats{};
+  stt.n_dof = n;
+  stt.nnz_stored = pl->nnz_operator;
+  stt.nnz_padded = pl->nnz_padded;
+  stt.n_interface = pl->n_int;
+  stt.n_direct_rows = pl->n_direct_rows;
+  if (prec == BFE_PREC_SINGLE && rs.n_sig > 0) stt.aux_launches += 1;
+  // optional per-launch CUDA-event timing: events are recorded around every
+  // launch on the launching stream and summed after the run
+  std::vector<cudaEvent_t> ev_step, ev_aux;
+  auto mark = [&](std::vector<cudaEvent_t>& v) -> cudaError_t {
+    cudaEvent_t e;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return r;
+    v.push_back(e);
+    return cudaEventRecord(e, st);
+  };
+  struct EvGuard {
+    std::vector<cudaEvent_t>* a; std::vector<cudaEvent_t>* b;
+    ~EvGuard() { for (auto e : *a) cudaEventDestroy(e); for (auto e : *b) cudaEventDestroy(e); }
+  } guard{&ev_step, &ev_aux};
+  const bool timing = pl->timing;
   for (int64_t ti = rs.ti_start; ti < rs.n_t; ++ti) {
     a.ti = ti;
     a.u_prev = U[iprev];
     a.u_n = U[icur];
     a.u_new = U[inew];
+    if (timing) CUDA_TRY(mark(ev_step));
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
                            : bfe::launch_step_batched(a, prec, pl->max_slice_entries, st);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
+    if (timing) CUDA_TRY(mark(ev_step));
+    stt.step_launches++;
     if (pl->n_int) {
+      if (timing) CUDA_TRY(mark(ev_aux));
       e = bfe::launch_interface_fixup(a, prec, st);
       if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "interface kernel launch failed: %s", cudaGetErrorString(e));
+      if (timing) CUDA_TRY(mark(ev_aux));
+      stt.aux_launches++;
     }
     if (rs.every_n > 0 && rs.d_fld && ti % rs.every_n == 0) {
       const int64_t k = ti / rs.every_n;
+      if (timing) CUDA_TRY(mark(ev_aux));
       e = bfe::launch_frame(a, prec, rs.d_fld, k, rs.field_is_vel, pl->dt, st);
       if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "frame kernel launch failed: %s", cudaGetErrorString(e));
+      if (timing) CUDA_TRY(mark(ev_aux));
+      stt.aux_launches++;
       if (rs.fld_time) (*rs.fld_time)[k] = rs.time[ti];
     }
     const int t = iprev;
     iprev = icur;
     icur = inew;
     inew = t;
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  for (size_t k = 0; k + 1 < ev_step.size(); k += 2) {
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, ev_step[k], ev_step[k + 1]));
+    stt.step_ms += ms;
+  }
+  for (size_t k = 0; k + 1 < ev_aux.size(); k += 2) {
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, ev_aux[k], ev_aux[k + 1]));
+    stt.aux_ms += ms;
   }
   CUDA_TRY(cudaStreamSynchronize(st));
   return BFE_OK;

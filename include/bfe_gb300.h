@@ -148,6 +148,26 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
                    int64_t q, const int64_t* hist_idx, double* d_hist,
                    void* stream);
 
+/* Counters of a plan's last run (no reference counterpart; used by the
+ * benchmark for its roofline and launch-count figures). */
+typedef struct bfe_stats {
+  int64_t step_launches;     /* time-step kernel launches in the last run */
+  int64_t aux_launches;      /* interface / frame / conversion launches */
+  double step_ms;            /* summed device time of the step kernels (timing on) */
+  double aux_ms;             /* summed device time of the other launches (timing on) */
+  int64_t n_dof;             /* rows of the operator */
+  int64_t nnz_stored;        /* operator entries kept (without padding) */
+  int64_t nnz_padded;        /* operator entries including sliced-ELL padding */
+  int64_t n_interface;       /* rows with fluid-solid coupling */
+  int64_t n_direct_rows;     /* FP32 rows evaluated in direct form */
+} bfe_stats;
+
+/* Enable (1) or disable (0) CUDA-event timing of every launch in later runs. */
+int bfe_plan_set_timing(bfe_plan* plan, int32_t enable);
+
+/* Copy the counters of the plan's last run. */
+int bfe_plan_stats(const bfe_plan* plan, bfe_stats* out);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* bfe_last_error(void);
 
