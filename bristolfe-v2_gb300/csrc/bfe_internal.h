@@ -69,8 +69,10 @@ struct StepArgs {
 
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.
 cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
+// Number of kernel variants the autotuner may choose from for (precision, R).
+int batched_variants(int precision, int R);
 cudaError_t launch_step_batched(const StepArgs& a, int precision, int max_slice_entries,
-                                cudaStream_t s);                                      // any R
+                                int variant, cudaStream_t s);                         // any R
 size_t batched_smem_bytes(int precision, int max_slice_entries);
 cudaError_t set_batched_smem_limit(int precision, size_t smem);
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);

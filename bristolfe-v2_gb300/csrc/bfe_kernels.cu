@@ -228,6 +228,96 @@ __global__ void __launch_bounds__(256) step_batched(StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// FP32 batched fast path (R a multiple of 64). A half-warp owns one row and
+// 64 right-hand sides as one float4 per lane, so every gathered state row is
+// one contiguous 256-byte segment and a warp streams two rows at once. The
+// row's entry words are read directly from the column-major slice (both
+// half-warps of a warp read neighbouring words, one sector), the reference
+// values of the row's own node block (difference form) are loaded once per
+// row, and the gathers are issued eight entries deep before the FMAs.
+template <int UNROLL, int MINB>
+__global__ void __launch_bounds__(256, MINB) step_f32_x64(StepArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int half = lane >> 4;
+  const int hl = lane & 15;
+  const int i = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + half;
+  if (i >= a.n) return;
+  const int s = i >> 5, rr = i & 31;
+  const int off = __ldg(a.slice_ptr + s);
+  const int w = (__ldg(a.slice_ptr + s + 1) - off) >> 5;
+  const uint32_t* colp = a.col + off + rr;
+  const float* valp = static_cast<const float*>(a.val) + off + rr;
+  const uint32_t info = __ldg(a.rowinfo + i);
+  const uint32_t base = info & kBaseMask;
+  const int R = a.R;
+  const float* un = static_cast<const float*>(a.u_n);
+  const float* upv = static_cast<const float*>(a.u_prev);
+  float* unew = static_cast<float*>(a.u_new);
+  const float q = __ldg(static_cast<const float*>(a.rowc) + i);
+  const size_t nm1 = (size_t)a.n - 1;
+  for (int c = hl * 4; c < R; c += 64) {
+    // own node block values u[base + slot], slot 0..3 (clamped in range)
+    float4 r0 = __ldg(reinterpret_cast<const float4*>(un + min((size_t)base + 0, nm1) * R + c));
+    float4 r1 = __ldg(reinterpret_cast<const float4*>(un + min((size_t)base + 1, nm1) * R + c));
+    float4 r2 = __ldg(reinterpret_cast<const float4*>(un + min((size_t)base + 2, nm1) * R + c));
+    float4 r3 = __ldg(reinterpret_cast<const float4*>(un + min((size_t)base + 3, nm1) * R + c));
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k0 = 0; k0 < w; k0 += UNROLL) {
+      uint32_t e[UNROLL];
+      float lv[UNROLL];
+      float4 uj[UNROLL];
+#pragma unroll
+      for (int t = 0; t < UNROLL; ++t) {
+        const bool ok = k0 + t < w;
+        e[t] = ok ? __ldg(colp + 32 * (k0 + t)) : (kDirect | (uint32_t)i);
+        lv[t] = ok ? __ldg(valp + 32 * (k0 + t)) : 0.f;
+      }
+#pragma unroll
+      for (int t = 0; t < UNROLL; ++t)
+        uj[t] = __ldg(reinterpret_cast<const float4*>(un + (size_t)(e[t] & kColMask) * R + c));
+#pragma unroll
+      for (int t = 0; t < UNROLL; ++t) {
+        const uint32_t sl = (e[t] >> kSlotShift) & kSlotMask;
+        float4 ur = sl == 0 ? r0 : sl == 1 ? r1 : sl == 2 ? r2 : r3;
+        if (e[t] & kDirect) ur = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (sl > 3 && !(e[t] & kDirect))
+          ur = __ldg(reinterpret_cast<const float4*>(un + ((size_t)base + sl) * R + c));
+        acc.x = fmaf(lv[t], uj[t].x - ur.x, acc.x);
+        acc.y = fmaf(lv[t], uj[t].y - ur.y, acc.y);
+        acc.z = fmaf(lv[t], uj[t].z - ur.z, acc.z);
+        acc.w = fmaf(lv[t], uj[t].w - ur.w, acc.w);
+      }
+    }
+    const size_t o = (size_t)i * R + c;
+    const float4 ui = __ldg(reinterpret_cast<const float4*>(un + o));
+    const float4 up = __ldcs(reinterpret_cast<const float4*>(upv + o));
+    float res[4], vint[4];
+    const float uiv[4] = {ui.x, ui.y, ui.z, ui.w};
+    const float upvv[4] = {up.x, up.y, up.z, up.w};
+    const float accv[4] = {acc.x, acc.y, acc.z, acc.w};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      float d, err;
+      two_sum(uiv[v], -upvv[v], d, err);
+      float inc = fmaf(q, d, -accv[v]);
+      if (info & kRowForced) inc += forcing_sum<float>(a, i, c + v);
+      inc = fmaf(q, err, inc);
+      res[v] = uiv[v] + inc;
+      vint[v] = a.int_base_prev ? (d + err + inc) : (d + err);
+    }
+    *reinterpret_cast<float4*>(unew + o) = make_float4(res[0], res[1], res[2], res[3]);
+    if (info & kRowInterface) {
+      const int t = lower_bound_i32(a.int_row, a.n_int, i);
+      *reinterpret_cast<float4*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) =
+          make_float4(vint[0], vint[1], vint[2], vint[3]);
+    } else if (info & kRowMonitored) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) write_history(a, i, c + v, (double)res[v]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
 template <typename T>
@@ -280,15 +370,27 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
   return ((size_t(max_slice_entries) * 4 + 15) & ~size_t(15)) + size_t(max_slice_entries) * elem;
 }
 
+int batched_variants(int precision, int R) {
+  return (precision == 1 && R % 64 == 0) ? 4 : 1;
+}
+
 cudaError_t launch_step_batched(const StepArgs& a, int precision, int max_slice_entries,
-                                cudaStream_t st) {
+                                int variant, cudaStream_t st) {
   const int threads = 256;
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
+  } else if (a.R % 64 == 0) {
+    const int rows_per_block = threads / 16;
+    const int grid = (a.n + rows_per_block - 1) / rows_per_block;
+    switch (variant) {
+      case 0: step_f32_x64<8, 2><<<grid, threads, 0, st>>>(a); break;
+      case 1: step_f32_x64<4, 3><<<grid, threads, 0, st>>>(a); break;
+      case 2: step_f32_x64<8, 3><<<grid, threads, 0, st>>>(a); break;
+      default: step_f32_x64<4, 4><<<grid, threads, 0, st>>>(a); break;
+    }
   } else {
-    if (a.R % 64 == 0) step_batched<float, 2><<<a.n_slices, threads, smem, st>>>(a);
-    else step_batched<float, 1><<<a.n_slices, threads, smem, st>>>(a);
+    step_batched<float, 1><<<a.n_slices, threads, smem, st>>>(a);
   }
   return cudaGetLastError();
 }

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -231,6 +232,8 @@ struct bfe_plan {
   int64_t n_direct_rows = 0;
   bool timing = false;
   bfe_stats last{};
+  // autotuned batched-kernel variant per R (chosen on the first run with that R)
+  std::map<int64_t, int> variant_of_R;
 };
 
 namespace {
@@ -696,6 +699,48 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     ~EvGuard() { for (auto e : *a) cudaEventDestroy(e); for (auto e : *b) cudaEventDestroy(e); }
   } guard{&ev_step, &ev_aux};
   const bool timing = pl->timing;
+  // Autotuner: on the first batched run with this R, time every kernel
+  // variant on a few steps of the real operator (state still zero, so the
+  // results are discarded by the real march that follows) and keep the
+  // fastest. BFE_VARIANT=<k> forces variant k (for sweeps).
+  int variant = 0;
+  if (R > 1) {
+    const int nv = bfe::batched_variants(prec, (int)R);
+    auto it = pl->variant_of_R.find(R);
+    const char* force = getenv("BFE_VARIANT");
+    if (force && nv > 1) {
+      variant = std::max(0, std::min(nv - 1, atoi(force)));
+    } else if (it != pl->variant_of_R.end()) {
+      variant = it->second;
+    } else if (nv > 1 && rs.ti_start < rs.n_t) {
+      a.ti = rs.ti_start;
+      a.u_prev = U[0];
+      a.u_n = U[1];
+      a.u_new = U[2];
+      cudaEvent_t e0, e1;
+      CUDA_TRY(cudaEventCreate(&e0));
+      CUDA_TRY(cudaEventCreate(&e1));
+      float best = 1e30f;
+      for (int v = 0; v < nv; ++v) {
+        CUDA_TRY(bfe::launch_step_batched(a, prec, pl->max_slice_entries, v, st));   // warm
+        CUDA_TRY(cudaEventRecord(e0, st));
+        for (int k = 0; k < 3; ++k) CUDA_TRY(bfe::launch_step_batched(a, prec, pl->max_slice_entries, v, st));
+        CUDA_TRY(cudaEventRecord(e1, st));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) { best = ms; variant = v; }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * state_bytes, st));
+      if (rs.d_hist && rs.hist_idx.size()) {
+        // the tuning launches wrote zero history at ti_start; nothing to undo
+      }
+      pl->variant_of_R[R] = variant;
+    }
+  }
+  stt.variant = variant;
   for (int64_t ti = rs.ti_start; ti < rs.n_t; ++ti) {
     a.ti = ti;
     a.u_prev = U[iprev];
@@ -703,7 +748,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     a.u_new = U[inew];
     if (timing) CUDA_TRY(mark(ev_step));
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, prec, pl->max_slice_entries, st);
+                           : bfe::launch_step_batched(a, prec, pl->max_slice_entries, variant, st);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (timing) CUDA_TRY(mark(ev_step));
     stt.step_launches++;

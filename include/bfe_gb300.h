@@ -160,6 +160,7 @@ typedef struct bfe_stats {
   int64_t nnz_padded;        /* operator entries including sliced-ELL padding */
   int64_t n_interface;       /* rows with fluid-solid coupling */
   int64_t n_direct_rows;     /* FP32 rows evaluated in direct form */
+  int64_t variant;           /* batched kernel variant chosen by the autotuner */
 } bfe_stats;
 
 /* Enable (1) or disable (0) CUDA-event timing of every launch in later runs. */
