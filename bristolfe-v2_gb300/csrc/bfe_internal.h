@@ -67,12 +67,32 @@ struct StepArgs {
   int64_t ti;                 // 0-based time index of the computed state
 };
 
+// Node-block operator (FP32 difference form): all DOF rows of one mesh node
+// are produced together from the neighbour node blocks.
+//   node_word[a]  = base row of node a (bits 0-29) | (rows - 1) << 30
+//   nbr_ptr[a]    = first neighbour entry of node a (n_nodes + 1 entries)
+//   nbr[e]        = {base row of neighbour block, meta}, meta bits 0-1 =
+//                   rows of the neighbour block - 1, bits 2+2k..3+2k = slot
+//                   (in node a's block) of the DOF type of neighbour row k
+//   coef_ptr[a]   = first coefficient of node a; per neighbour block the
+//                   coefficients are row-major [own row][neighbour row]
+struct NodeArgs {
+  int32_t n_nodes;
+  const uint32_t* node_word;
+  const int32_t* nbr_ptr;
+  const uint2* nbr;
+  const int32_t* coef_ptr;
+  const float* coef;
+  int32_t max_nbr;            // largest neighbour count of a node
+  int32_t max_coef;           // largest coefficient count of a node
+};
+
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.
 cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
 // Number of kernel variants the autotuner may choose from for (precision, R).
-int batched_variants(int precision, int R);
-cudaError_t launch_step_batched(const StepArgs& a, int precision, int max_slice_entries,
-                                int variant, cudaStream_t s);                         // any R
+int batched_variants(int precision, int R, bool have_nodes);
+cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, int precision,
+                                int max_slice_entries, int variant, cudaStream_t s);   // any R
 size_t batched_smem_bytes(int precision, int max_slice_entries);
 cudaError_t set_batched_smem_limit(int precision, size_t smem);
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);

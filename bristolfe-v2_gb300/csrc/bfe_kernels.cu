@@ -318,6 +318,117 @@ __global__ void __launch_bounds__(256, MINB) step_f32_x64(StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// FP32 node-block kernel (R a multiple of 64). One warp per mesh node: the
+// node's neighbour words and coefficients are copied into the warp's slice of
+// shared memory with coalesced loads, the node's own DOF values (the
+// difference-form references) are kept in registers, and every neighbour
+// block's R-vectors are gathered once and applied to all of the node's rows.
+// Lanes own two right-hand sides each (float2), so a gathered state row is
+// one 256-byte segment per warp.
+constexpr int kNodeWarps = 8;
+constexpr int kNodeNbr = 64;     // neighbour words staged per warp per pass
+constexpr int kNodeCoef = 288;   // coefficients staged per warp per pass
+
+template <int MAXNB>
+__global__ void __launch_bounds__(256) step_f32_node(StepArgs a, NodeArgs g) {
+  __shared__ uint2 s_nbr[kNodeWarps][kNodeNbr];
+  __shared__ float s_coef[kNodeWarps][kNodeCoef];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  const int node = blockIdx.x * kNodeWarps + wid;
+  if (node >= g.n_nodes) return;
+  const uint32_t nw = __ldg(g.node_word + node);
+  const int base = (int)(nw & 0x3FFFFFFFu);
+  const int nb = (int)(nw >> 30) + 1;
+  const int p0 = __ldg(g.nbr_ptr + node), p1 = __ldg(g.nbr_ptr + node + 1);
+  const int cp0 = __ldg(g.coef_ptr + node), cp1 = __ldg(g.coef_ptr + node + 1);
+  const int R = a.R;
+  const float* un = static_cast<const float*>(a.u_n);
+  const float* upv = static_cast<const float*>(a.u_prev);
+  float* unew = static_cast<float*>(a.u_new);
+  // a node fits in one staging pass when its lists fit the warp's slice
+  const bool one_pass = (p1 - p0) <= kNodeNbr && (cp1 - cp0) <= kNodeCoef;
+  if (one_pass) {
+    for (int e = lane; e < p1 - p0; e += 32) s_nbr[wid][e] = __ldg(g.nbr + p0 + e);
+    for (int e = lane; e < cp1 - cp0; e += 32) s_coef[wid][e] = __ldg(g.coef + cp0 + e);
+    __syncwarp();
+  }
+  for (int c = lane * 2; c < R; c += 64) {
+    float2 uo[MAXNB];
+#pragma unroll
+    for (int s2 = 0; s2 < MAXNB; ++s2)
+      uo[s2] = s2 < nb ? __ldg(reinterpret_cast<const float2*>(un + (size_t)(base + s2) * R + c))
+                       : make_float2(0.f, 0.f);
+    float2 acc[MAXNB];
+#pragma unroll
+    for (int s2 = 0; s2 < MAXNB; ++s2) acc[s2] = make_float2(0.f, 0.f);
+    int cp = 0;
+    for (int e = 0; e < p1 - p0; ++e) {
+      const uint2 wv = one_pass ? s_nbr[wid][e] : __ldg(g.nbr + p0 + e);
+      const int nbj = (int)(wv.y & 3u) + 1;
+      float2 d[MAXNB];
+#pragma unroll
+      for (int k = 0; k < MAXNB; ++k) {
+        if (k < nbj) {
+          const int sl = (int)((wv.y >> (2 + 2 * k)) & 3u);
+          const float2 uj = __ldg(reinterpret_cast<const float2*>(un + (size_t)(wv.x + k) * R + c));
+          float2 ur = uo[0];
+#pragma unroll
+          for (int s2 = 1; s2 < MAXNB; ++s2) if (sl == s2) ur = uo[s2];
+          d[k] = make_float2(uj.x - ur.x, uj.y - ur.y);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < MAXNB; ++i) {
+        if (i < nb) {
+#pragma unroll
+          for (int k = 0; k < MAXNB; ++k) {
+            if (k < nbj) {
+              const float cv = one_pass ? s_coef[wid][cp + i * nbj + k] : __ldg(g.coef + cp0 + cp + i * nbj + k);
+              acc[i].x = fmaf(cv, d[k].x, acc[i].x);
+              acc[i].y = fmaf(cv, d[k].y, acc[i].y);
+            }
+          }
+        }
+      }
+      cp += nb * nbj;
+    }
+#pragma unroll
+    for (int i = 0; i < MAXNB; ++i) {
+      if (i >= nb) break;
+      const int row = base + i;
+      const uint32_t info = __ldg(a.rowinfo + row);
+      const float q = __ldg(static_cast<const float*>(a.rowc) + row);
+      const size_t o = (size_t)row * R + c;
+      const float2 up = __ldcs(reinterpret_cast<const float2*>(upv + o));
+      const float uiv[2] = {uo[i].x, uo[i].y};
+      const float upvv[2] = {up.x, up.y};
+      const float accv[2] = {acc[i].x, acc[i].y};
+      float res[2], vint[2];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        float dd, err;
+        two_sum(uiv[v], -upvv[v], dd, err);
+        float inc = fmaf(q, dd, -accv[v]);
+        if (info & kRowForced) inc += forcing_sum<float>(a, row, c + v);
+        inc = fmaf(q, err, inc);
+        res[v] = uiv[v] + inc;
+        vint[v] = a.int_base_prev ? (dd + err + inc) : (dd + err);
+      }
+      *reinterpret_cast<float2*>(unew + o) = make_float2(res[0], res[1]);
+      if (info & kRowInterface) {
+        const int t = lower_bound_i32(a.int_row, a.n_int, row);
+        *reinterpret_cast<float2*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) =
+            make_float2(vint[0], vint[1]);
+      } else if (info & kRowMonitored) {
+        write_history(a, row, c, (double)res[0]);
+        write_history(a, row, c + 1, (double)res[1]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
 template <typename T>
@@ -370,24 +481,32 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
   return ((size_t(max_slice_entries) * 4 + 15) & ~size_t(15)) + size_t(max_slice_entries) * elem;
 }
 
-int batched_variants(int precision, int R) {
-  return (precision == 1 && R % 64 == 0) ? 4 : 1;
+// Variants for the autotuner. FP32 with R % 64 == 0: 0 = slice-staged
+// row kernel, 1..3 = half-warp float4 row kernels, 4 = node-block kernel
+// (only when the plan has node blocks).
+int batched_variants(int precision, int R, bool have_nodes) {
+  if (precision == 1 && R % 64 == 0) return have_nodes ? 5 : 4;
+  return 1;
 }
 
-cudaError_t launch_step_batched(const StepArgs& a, int precision, int max_slice_entries,
-                                int variant, cudaStream_t st) {
+cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, int precision,
+                                int max_slice_entries, int variant, cudaStream_t st) {
   const int threads = 256;
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
+  } else if (a.R % 64 == 0 && variant == 4 && g) {
+    const int grid = (g->n_nodes + kNodeWarps - 1) / kNodeWarps;
+    step_f32_node<3><<<grid, kNodeWarps * 32, 0, st>>>(a, *g);
+  } else if (a.R % 64 == 0 && variant == 0) {
+    step_batched<float, 2><<<a.n_slices, threads, smem, st>>>(a);
   } else if (a.R % 64 == 0) {
     const int rows_per_block = threads / 16;
     const int grid = (a.n + rows_per_block - 1) / rows_per_block;
     switch (variant) {
-      case 0: step_f32_x64<8, 2><<<grid, threads, 0, st>>>(a); break;
-      case 1: step_f32_x64<4, 3><<<grid, threads, 0, st>>>(a); break;
-      case 2: step_f32_x64<8, 3><<<grid, threads, 0, st>>>(a); break;
-      default: step_f32_x64<4, 4><<<grid, threads, 0, st>>>(a); break;
+      case 1: step_f32_x64<4, 4><<<grid, threads, 0, st>>>(a); break;
+      case 2: step_f32_x64<4, 3><<<grid, threads, 0, st>>>(a); break;
+      default: step_f32_x64<8, 2><<<grid, threads, 0, st>>>(a); break;
     }
   } else {
     step_batched<float, 1><<<a.n_slices, threads, smem, st>>>(a);

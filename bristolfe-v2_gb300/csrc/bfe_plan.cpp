@@ -234,6 +234,25 @@ struct bfe_plan {
   bfe_stats last{};
   // autotuned batched-kernel variant per R (chosen on the first run with that R)
   std::map<int64_t, int> variant_of_R;
+  // node-block operator (FP32 difference form with node information)
+  bool have_node_blocks = false;
+  int32_t n_nodes = 0, max_nbr = 0, max_coef = 0;
+  DevBuf<uint32_t> node_word;
+  DevBuf<int32_t> nbr_ptr, coef_ptr;
+  DevBuf<uint2> nbr;
+  DevBuf<float> coef;
+  bfe::NodeArgs node_args() const {
+    bfe::NodeArgs g{};
+    g.n_nodes = n_nodes;
+    g.node_word = node_word.p;
+    g.nbr_ptr = nbr_ptr.p;
+    g.nbr = nbr.p;
+    g.coef_ptr = coef_ptr.p;
+    g.coef = coef.p;
+    g.max_nbr = max_nbr;
+    g.max_coef = max_coef;
+    return g;
+  }
 };
 
 namespace {
@@ -523,6 +542,78 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
     if (hcol.size() > (size_t)INT32_MAX) return fail(BFE_ERR_UNSUPPORTED, "operator too large for 32-bit offsets");
     pl->max_slice_entries = std::max<int32_t>(pl->max_slice_entries, (int32_t)(w * bfe::kSlice));
   }
+  // Node-block form of the FP32 operator: every row must use the difference
+  // form, node blocks must hold at most 3 DOFs, and every non-zero coupling
+  // to a neighbour DOF type must exist in the own block.
+  if (precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0) {
+    bool ok = true;
+    std::vector<uint32_t> hw;
+    std::vector<int32_t> hnp(1, 0), hcp(1, 0);
+    std::vector<uint2> hn;
+    std::vector<float> hc;
+    int32_t max_nbr = 0, max_coef = 0;
+    int64_t b = 0;
+    std::vector<int64_t> nbr_bases;
+    while (b < n && ok) {
+      const int64_t nb = blk_len[b];
+      if (nb > 3 || b > 0x3FFFFFFF) { ok = false; break; }
+      hw.push_back((uint32_t)b | ((uint32_t)(nb - 1) << 30));
+      nbr_bases.clear();
+      for (int64_t i = b; i < b + nb; ++i)
+        for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e)
+          if (dof_node[K.idx[e]] != dof_node[b]) nbr_bases.push_back(blk_base[K.idx[e]]);
+      std::sort(nbr_bases.begin(), nbr_bases.end());
+      nbr_bases.erase(std::unique(nbr_bases.begin(), nbr_bases.end()), nbr_bases.end());
+      int32_t ncoef = 0;
+      for (int64_t bb : nbr_bases) {
+        const int64_t nbj = blk_len[bb];
+        if (nbj > 3) { ok = false; break; }
+        uint32_t meta = (uint32_t)(nbj - 1);
+        // coefficients [own row i][neighbour row k]
+        for (int64_t i = 0; i < nb; ++i) {
+          const int64_t row = b + i;
+          for (int64_t k = 0; k < nbj; ++k) {
+            const int64_t colj = bb + k;
+            const int64_t* beg = K.idx.data() + K.ptr[row];
+            const int64_t* end = K.idx.data() + K.ptr[row + 1];
+            const int64_t* hit = std::lower_bound(beg, end, colj);
+            const double v = (hit != end && *hit == colj) ? lscale[row] * K.val[hit - K.idx.data()] : 0.0;
+            hc.push_back((float)v);
+          }
+        }
+        for (int64_t k = 0; k < nbj; ++k) {
+          int64_t slot = -1;
+          for (int64_t t = 0; t < nb; ++t)
+            if (dof_type[b + t] == dof_type[bb + k]) slot = t;
+          if (slot < 0) {
+            // no own DOF of that type: allowed only if the whole column is zero
+            for (int64_t i = 0; i < nb; ++i)
+              if (hc[hc.size() - nb * nbj + i * nbj + k] != 0.0f) ok = false;
+            slot = 0;
+          }
+          meta |= (uint32_t)slot << (2 + 2 * k);
+        }
+        hn.push_back(make_uint2((uint32_t)bb, meta));
+        ncoef += (int32_t)(nb * nbj);
+      }
+      max_nbr = std::max<int32_t>(max_nbr, (int32_t)nbr_bases.size());
+      max_coef = std::max(max_coef, ncoef);
+      hnp.push_back((int32_t)hn.size());
+      hcp.push_back((int32_t)hc.size());
+      b += nb;
+    }
+    if (ok && hc.size() < (size_t)INT32_MAX) {
+      pl->have_node_blocks = true;
+      pl->n_nodes = (int32_t)hw.size();
+      pl->max_nbr = max_nbr;
+      pl->max_coef = max_coef;
+      CUDA_TRY(pl->node_word.upload(hw));
+      CUDA_TRY(pl->nbr_ptr.upload(hnp));
+      CUDA_TRY(pl->coef_ptr.upload(hcp));
+      CUDA_TRY(pl->nbr.upload(hn));
+      CUDA_TRY(pl->coef.upload(hc));
+    }
+  }
   pl->nnz_operator = stored;
   pl->nnz_padded = (int64_t)hcol.size();
   pl->n_direct_rows = direct_rows;
@@ -683,6 +774,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   stt.nnz_padded = pl->nnz_padded;
   stt.n_interface = pl->n_int;
   stt.n_direct_rows = pl->n_direct_rows;
+  stt.n_nodes = pl->have_node_blocks ? pl->n_nodes : 0;
   if (prec == BFE_PREC_SINGLE && rs.n_sig > 0) stt.aux_launches += 1;
   // optional per-launch CUDA-event timing: events are recorded around every
   // launch on the launching stream and summed after the run
@@ -704,8 +796,10 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   // results are discarded by the real march that follows) and keep the
   // fastest. BFE_VARIANT=<k> forces variant k (for sweeps).
   int variant = 0;
+  const bfe::NodeArgs g = pl->node_args();
+  const bfe::NodeArgs* gp = pl->have_node_blocks ? &g : nullptr;
   if (R > 1) {
-    const int nv = bfe::batched_variants(prec, (int)R);
+    const int nv = bfe::batched_variants(prec, (int)R, pl->have_node_blocks);
     auto it = pl->variant_of_R.find(R);
     const char* force = getenv("BFE_VARIANT");
     if (force && nv > 1) {
@@ -722,9 +816,9 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       CUDA_TRY(cudaEventCreate(&e1));
       float best = 1e30f;
       for (int v = 0; v < nv; ++v) {
-        CUDA_TRY(bfe::launch_step_batched(a, prec, pl->max_slice_entries, v, st));   // warm
+        CUDA_TRY(bfe::launch_step_batched(a, gp, prec, pl->max_slice_entries, v, st));   // warm
         CUDA_TRY(cudaEventRecord(e0, st));
-        for (int k = 0; k < 3; ++k) CUDA_TRY(bfe::launch_step_batched(a, prec, pl->max_slice_entries, v, st));
+        for (int k = 0; k < 3; ++k) CUDA_TRY(bfe::launch_step_batched(a, gp, prec, pl->max_slice_entries, v, st));
         CUDA_TRY(cudaEventRecord(e1, st));
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;
@@ -748,7 +842,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     a.u_new = U[inew];
     if (timing) CUDA_TRY(mark(ev_step));
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, prec, pl->max_slice_entries, variant, st);
+                           : bfe::launch_step_batched(a, gp, prec, pl->max_slice_entries, variant, st);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (timing) CUDA_TRY(mark(ev_step));
     stt.step_launches++;

@@ -168,3 +168,27 @@ def test_errors_through_the_abi(bfe, plate):
             plan.run(t * 2, [1], np.ones(20), [1])                 # dt mismatch
         with pytest.raises(bfe.BfeError):
             plan.run(t, [1, 2], np.ones((3, 20)), [1])             # 3 rows for 2 DOFs
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
+    """Each kernel the autotuner can pick (forced through BFE_VARIANT) gives
+    the same answers; variant 4 is the node-block kernel."""
+    m = coupled
+    nt = 150
+    t, s = modelgen.pulse(nt, m["dt"])
+    nds = np.nonzero(m["gl"][:, 3] > 0)[0] + 1
+    srcs = [modelgen.gi_of(m["gl"], [nds[(11 * r) % nds.size]], 4) for r in range(64)]
+    hi = np.concatenate([modelgen.gi_of(m["gl"], m["mon_nds"], 4),
+                         modelgen.gi_of(m["gl"], m["mon_nds"], 2)])
+    q4 = modelgen.gi_of(m["gl"], m["mon_nds"], 4).size
+    monkeypatch.setenv("BFE_VARIANT", str(variant))
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, "single", m["gl"]) as plan:
+        hb = plan.run_batched(t, srcs, s, hi)
+        st = plan.stats()
+    assert st["variant"] == variant
+    assert st["n_nodes"] > 0
+    for r in (0, 33):
+        h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
+        assert _err(hb[:q4, :, r], h0[:q4]) <= TOL32
+        assert _err(hb[q4:, :, r], h0[q4:]) <= TOL32
