@@ -68,19 +68,18 @@ struct StepArgs {
 };
 
 // Node-block operator (FP32 difference form): all DOF rows of one mesh node
-// are produced together from the neighbour node blocks.
+// are produced together from the neighbour DOF rows they couple to.
 //   node_word[a]  = base row of node a (bits 0-29) | (rows - 1) << 30
-//   nbr_ptr[a]    = first neighbour entry of node a (n_nodes + 1 entries)
-//   nbr[e]        = {base row of neighbour block, meta}, meta bits 0-1 =
-//                   rows of the neighbour block - 1, bits 2+2k..3+2k = slot
-//                   (in node a's block) of the DOF type of neighbour row k
-//   coef_ptr[a]   = first coefficient of node a; per neighbour block the
-//                   coefficients are row-major [own row][neighbour row]
+//   nbr_ptr[a]    = first gathered row of node a (n_nodes + 1 entries)
+//   gword[e]      = gathered row (bits 0-27) | slot << 28, slot = position in
+//                   node a's block of the DOF with the gathered row's type
+//   coef_ptr[a]   = first coefficient of node a; coefficients are
+//                   [gathered row][own row]
 struct NodeArgs {
   int32_t n_nodes;
   const uint32_t* node_word;
   const int32_t* nbr_ptr;
-  const uint2* nbr;
+  const uint32_t* gword;
   const int32_t* coef_ptr;
   const float* coef;
   int32_t max_nbr;            // largest neighbour count of a node

@@ -318,20 +318,20 @@ __global__ void __launch_bounds__(256, MINB) step_f32_x64(StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// FP32 node-block kernel (R a multiple of 64). One warp per mesh node: the
-// node's neighbour words and coefficients are copied into the warp's slice of
-// shared memory with coalesced loads, the node's own DOF values (the
-// difference-form references) are kept in registers, and every neighbour
-// block's R-vectors are gathered once and applied to all of the node's rows.
-// Lanes own two right-hand sides each (float2), so a gathered state row is
-// one 256-byte segment per warp.
+// FP32 node-block kernel (R a multiple of 64). One warp per mesh node: every
+// neighbour DOF row the node needs is gathered once (an R-vector, 256 bytes
+// per warp) and applied to all of the node's rows; the node's own DOF values
+// (the difference-form references) stay in registers. The node's gathered-row
+// words and coefficients are staged in the warp's slice of shared memory with
+// coalesced loads, and gathers are issued UNROLL rows deep before the FMAs so
+// that each warp keeps several KB in flight.
 constexpr int kNodeWarps = 8;
-constexpr int kNodeNbr = 64;     // neighbour words staged per warp per pass
-constexpr int kNodeCoef = 288;   // coefficients staged per warp per pass
+constexpr int kNodeG = 64;       // gathered-row words staged per warp
+constexpr int kNodeCoef = 192;   // coefficients staged per warp
 
-template <int MAXNB>
+template <int MAXNB, int UNROLL>
 __global__ void __launch_bounds__(256) step_f32_node(StepArgs a, NodeArgs g) {
-  __shared__ uint2 s_nbr[kNodeWarps][kNodeNbr];
+  __shared__ uint32_t s_w[kNodeWarps][kNodeG];
   __shared__ float s_coef[kNodeWarps][kNodeCoef];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
@@ -341,16 +341,16 @@ __global__ void __launch_bounds__(256) step_f32_node(StepArgs a, NodeArgs g) {
   const int base = (int)(nw & 0x3FFFFFFFu);
   const int nb = (int)(nw >> 30) + 1;
   const int p0 = __ldg(g.nbr_ptr + node), p1 = __ldg(g.nbr_ptr + node + 1);
-  const int cp0 = __ldg(g.coef_ptr + node), cp1 = __ldg(g.coef_ptr + node + 1);
+  const int G = p1 - p0;
+  const int cp0 = __ldg(g.coef_ptr + node);
   const int R = a.R;
   const float* un = static_cast<const float*>(a.u_n);
   const float* upv = static_cast<const float*>(a.u_prev);
   float* unew = static_cast<float*>(a.u_new);
-  // a node fits in one staging pass when its lists fit the warp's slice
-  const bool one_pass = (p1 - p0) <= kNodeNbr && (cp1 - cp0) <= kNodeCoef;
-  if (one_pass) {
-    for (int e = lane; e < p1 - p0; e += 32) s_nbr[wid][e] = __ldg(g.nbr + p0 + e);
-    for (int e = lane; e < cp1 - cp0; e += 32) s_coef[wid][e] = __ldg(g.coef + cp0 + e);
+  const bool staged = G <= kNodeG && G * nb <= kNodeCoef;
+  if (staged) {
+    for (int e = lane; e < G; e += 32) s_w[wid][e] = __ldg(g.gword + p0 + e);
+    for (int e = lane; e < G * nb; e += 32) s_coef[wid][e] = __ldg(g.coef + cp0 + e);
     __syncwarp();
   }
   for (int c = lane * 2; c < R; c += 64) {
@@ -362,36 +362,34 @@ __global__ void __launch_bounds__(256) step_f32_node(StepArgs a, NodeArgs g) {
     float2 acc[MAXNB];
 #pragma unroll
     for (int s2 = 0; s2 < MAXNB; ++s2) acc[s2] = make_float2(0.f, 0.f);
-    int cp = 0;
-    for (int e = 0; e < p1 - p0; ++e) {
-      const uint2 wv = one_pass ? s_nbr[wid][e] : __ldg(g.nbr + p0 + e);
-      const int nbj = (int)(wv.y & 3u) + 1;
-      float2 d[MAXNB];
+    for (int g0 = 0; g0 < G; g0 += UNROLL) {
+      uint32_t w[UNROLL];
+      float2 uj[UNROLL];
 #pragma unroll
-      for (int k = 0; k < MAXNB; ++k) {
-        if (k < nbj) {
-          const int sl = (int)((wv.y >> (2 + 2 * k)) & 3u);
-          const float2 uj = __ldg(reinterpret_cast<const float2*>(un + (size_t)(wv.x + k) * R + c));
+      for (int t = 0; t < UNROLL; ++t) {
+        const int gi = g0 + t;
+        w[t] = gi < G ? (staged ? s_w[wid][gi] : __ldg(g.gword + p0 + gi)) : (uint32_t)base;
+        uj[t] = __ldg(reinterpret_cast<const float2*>(un + (size_t)(w[t] & kColMask) * R + c));
+      }
+#pragma unroll
+      for (int t = 0; t < UNROLL; ++t) {
+        const int gi = g0 + t;
+        if (gi < G) {
+          const int sl = (int)((w[t] >> kSlotShift) & kSlotMask);
           float2 ur = uo[0];
 #pragma unroll
           for (int s2 = 1; s2 < MAXNB; ++s2) if (sl == s2) ur = uo[s2];
-          d[k] = make_float2(uj.x - ur.x, uj.y - ur.y);
-        }
-      }
+          const float dx = uj[t].x - ur.x, dy = uj[t].y - ur.y;
 #pragma unroll
-      for (int i = 0; i < MAXNB; ++i) {
-        if (i < nb) {
-#pragma unroll
-          for (int k = 0; k < MAXNB; ++k) {
-            if (k < nbj) {
-              const float cv = one_pass ? s_coef[wid][cp + i * nbj + k] : __ldg(g.coef + cp0 + cp + i * nbj + k);
-              acc[i].x = fmaf(cv, d[k].x, acc[i].x);
-              acc[i].y = fmaf(cv, d[k].y, acc[i].y);
+          for (int i = 0; i < MAXNB; ++i) {
+            if (i < nb) {
+              const float cv = staged ? s_coef[wid][gi * nb + i] : __ldg(g.coef + cp0 + gi * nb + i);
+              acc[i].x = fmaf(cv, dx, acc[i].x);
+              acc[i].y = fmaf(cv, dy, acc[i].y);
             }
           }
         }
       }
-      cp += nb * nbj;
     }
 #pragma unroll
     for (int i = 0; i < MAXNB; ++i) {
@@ -483,9 +481,9 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 
 // Variants for the autotuner. FP32 with R % 64 == 0: 0 = slice-staged
 // row kernel, 1..3 = half-warp float4 row kernels, 4 = node-block kernel
-// (only when the plan has node blocks).
+// (only when the plan has node blocks), 5 = node-block kernel, deeper unroll.
 int batched_variants(int precision, int R, bool have_nodes) {
-  if (precision == 1 && R % 64 == 0) return have_nodes ? 5 : 4;
+  if (precision == 1 && R % 64 == 0) return have_nodes ? 6 : 4;
   return 1;
 }
 
@@ -495,9 +493,10 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, int precis
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
-  } else if (a.R % 64 == 0 && variant == 4 && g) {
+  } else if (a.R % 64 == 0 && (variant == 4 || variant == 5) && g) {
     const int grid = (g->n_nodes + kNodeWarps - 1) / kNodeWarps;
-    step_f32_node<3><<<grid, kNodeWarps * 32, 0, st>>>(a, *g);
+    if (variant == 4) step_f32_node<3, 8><<<grid, kNodeWarps * 32, 0, st>>>(a, *g);
+    else step_f32_node<3, 12><<<grid, kNodeWarps * 32, 0, st>>>(a, *g);
   } else if (a.R % 64 == 0 && variant == 0) {
     step_batched<float, 2><<<a.n_slices, threads, smem, st>>>(a);
   } else if (a.R % 64 == 0) {

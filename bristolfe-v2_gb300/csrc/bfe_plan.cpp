@@ -239,14 +239,14 @@ struct bfe_plan {
   int32_t n_nodes = 0, max_nbr = 0, max_coef = 0;
   DevBuf<uint32_t> node_word;
   DevBuf<int32_t> nbr_ptr, coef_ptr;
-  DevBuf<uint2> nbr;
+  DevBuf<uint32_t> gword;
   DevBuf<float> coef;
   bfe::NodeArgs node_args() const {
     bfe::NodeArgs g{};
     g.n_nodes = n_nodes;
     g.node_word = node_word.p;
     g.nbr_ptr = nbr_ptr.p;
-    g.nbr = nbr.p;
+    g.gword = gword.p;
     g.coef_ptr = coef_ptr.p;
     g.coef = coef.p;
     g.max_nbr = max_nbr;
@@ -547,58 +547,46 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   // to a neighbour DOF type must exist in the own block.
   if (precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0) {
     bool ok = true;
-    std::vector<uint32_t> hw;
+    std::vector<uint32_t> hw, hg;
     std::vector<int32_t> hnp(1, 0), hcp(1, 0);
-    std::vector<uint2> hn;
     std::vector<float> hc;
     int32_t max_nbr = 0, max_coef = 0;
     int64_t b = 0;
-    std::vector<int64_t> nbr_bases;
+    std::vector<int64_t> cols;
     while (b < n && ok) {
       const int64_t nb = blk_len[b];
       if (nb > 3 || b > 0x3FFFFFFF) { ok = false; break; }
       hw.push_back((uint32_t)b | ((uint32_t)(nb - 1) << 30));
-      nbr_bases.clear();
+      // every neighbour DOF row any of the node's rows couples to
+      cols.clear();
       for (int64_t i = b; i < b + nb; ++i)
         for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e)
-          if (dof_node[K.idx[e]] != dof_node[b]) nbr_bases.push_back(blk_base[K.idx[e]]);
-      std::sort(nbr_bases.begin(), nbr_bases.end());
-      nbr_bases.erase(std::unique(nbr_bases.begin(), nbr_bases.end()), nbr_bases.end());
-      int32_t ncoef = 0;
-      for (int64_t bb : nbr_bases) {
-        const int64_t nbj = blk_len[bb];
-        if (nbj > 3) { ok = false; break; }
-        uint32_t meta = (uint32_t)(nbj - 1);
-        // coefficients [own row i][neighbour row k]
+          if (dof_node[K.idx[e]] != dof_node[b]) cols.push_back(K.idx[e]);
+      std::sort(cols.begin(), cols.end());
+      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+      for (int64_t j : cols) {
+        int64_t slot = -1;
+        for (int64_t t = 0; t < nb; ++t)
+          if (dof_type[b + t] == dof_type[j]) slot = t;
+        bool any = false;
         for (int64_t i = 0; i < nb; ++i) {
           const int64_t row = b + i;
-          for (int64_t k = 0; k < nbj; ++k) {
-            const int64_t colj = bb + k;
-            const int64_t* beg = K.idx.data() + K.ptr[row];
-            const int64_t* end = K.idx.data() + K.ptr[row + 1];
-            const int64_t* hit = std::lower_bound(beg, end, colj);
-            const double v = (hit != end && *hit == colj) ? lscale[row] * K.val[hit - K.idx.data()] : 0.0;
-            hc.push_back((float)v);
-          }
+          const int64_t* beg = K.idx.data() + K.ptr[row];
+          const int64_t* end = K.idx.data() + K.ptr[row + 1];
+          const int64_t* hit = std::lower_bound(beg, end, j);
+          const double v = (hit != end && *hit == j) ? lscale[row] * K.val[hit - K.idx.data()] : 0.0;
+          any = any || v != 0.0;
+          hc.push_back((float)v);
         }
-        for (int64_t k = 0; k < nbj; ++k) {
-          int64_t slot = -1;
-          for (int64_t t = 0; t < nb; ++t)
-            if (dof_type[b + t] == dof_type[bb + k]) slot = t;
-          if (slot < 0) {
-            // no own DOF of that type: allowed only if the whole column is zero
-            for (int64_t i = 0; i < nb; ++i)
-              if (hc[hc.size() - nb * nbj + i * nbj + k] != 0.0f) ok = false;
-            slot = 0;
-          }
-          meta |= (uint32_t)slot << (2 + 2 * k);
+        if (slot < 0) {
+          if (any) ok = false;      // coupling to a type the node lacks
+          slot = 0;
         }
-        hn.push_back(make_uint2((uint32_t)bb, meta));
-        ncoef += (int32_t)(nb * nbj);
+        hg.push_back((uint32_t)j | ((uint32_t)slot << bfe::kSlotShift));
       }
-      max_nbr = std::max<int32_t>(max_nbr, (int32_t)nbr_bases.size());
-      max_coef = std::max(max_coef, ncoef);
-      hnp.push_back((int32_t)hn.size());
+      max_nbr = std::max<int32_t>(max_nbr, (int32_t)cols.size());
+      max_coef = std::max<int32_t>(max_coef, (int32_t)(cols.size() * nb));
+      hnp.push_back((int32_t)hg.size());
       hcp.push_back((int32_t)hc.size());
       b += nb;
     }
@@ -610,7 +598,7 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
       CUDA_TRY(pl->node_word.upload(hw));
       CUDA_TRY(pl->nbr_ptr.upload(hnp));
       CUDA_TRY(pl->coef_ptr.upload(hcp));
-      CUDA_TRY(pl->nbr.upload(hn));
+      CUDA_TRY(pl->gword.upload(hg));
       CUDA_TRY(pl->coef.upload(hc));
     }
   }

@@ -170,10 +170,10 @@ def test_errors_through_the_abi(bfe, plate):
             plan.run(t, [1, 2], np.ones((3, 20)), [1])             # 3 rows for 2 DOFs
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
     """Each kernel the autotuner can pick (forced through BFE_VARIANT) gives
-    the same answers; variant 4 is the node-block kernel."""
+    the same answers; variants 4 and 5 are the node-block kernel."""
     m = coupled
     nt = 150
     t, s = modelgen.pulse(nt, m["dt"])
