@@ -86,12 +86,30 @@ struct NodeArgs {
   int32_t max_coef;           // largest coefficient count of a node
 };
 
+// Group block-sparse operator (FP32 difference form). DOF types that K
+// couples form groups (2D solid {1,2}, fluid {4}, 3D solid {1,2,3}); every
+// node carrying a group holds its rows consecutively, so each group is a
+// block-sparse matrix with BS x BS blocks over its nodes. All groups are
+// processed by one launch; CTAs [blk_begin[g], blk_begin[g+1]) take group g.
+constexpr int kMaxGroups = 4;
+struct GroupArgs {
+  int32_t n_groups;
+  int32_t bs[kMaxGroups];            // block size of each group (1..3)
+  int32_t n_nodes[kMaxGroups];
+  int32_t blk_begin[kMaxGroups + 1];
+  const int32_t* row0[kMaxGroups];   // first row of the group block of each node
+  const int32_t* nptr[kMaxGroups];   // neighbour list of each node (n_nodes + 1)
+  const int32_t* nrow[kMaxGroups];   // first row of each neighbour block
+  const float* coef[kMaxGroups];     // BS*BS per neighbour block, [own k][neighbour l]
+};
+
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.
 cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
 // Number of kernel variants the autotuner may choose from for (precision, R).
-int batched_variants(int precision, int R, bool have_nodes);
-cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, int precision,
-                                int max_slice_entries, int variant, cudaStream_t s);   // any R
+int batched_variants(int precision, int R, bool have_nodes, bool have_groups);
+cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const GroupArgs* gr,
+                                int precision, int max_slice_entries, int variant,
+                                cudaStream_t s);                                      // any R
 size_t batched_smem_bytes(int precision, int max_slice_entries);
 cudaError_t set_batched_smem_limit(int precision, size_t smem);
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);

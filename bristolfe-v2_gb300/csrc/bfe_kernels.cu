@@ -427,6 +427,125 @@ __global__ void __launch_bounds__(256) step_f32_node(StepArgs a, NodeArgs g) {
 }
 
 // ---------------------------------------------------------------------------
+// FP32 group block-sparse kernel (R a multiple of 64). One warp per node of a
+// group; lanes own two right-hand sides (float2). For every neighbour block
+// the warp gathers BS state rows (256 bytes each), forms the differences with
+// the node's own block (kept in registers) and applies the BS x BS
+// coefficient block, read with one broadcast load. UNROLL neighbour blocks
+// are gathered before their FMAs.
+template <int BS>
+struct CoefBlock { float v[BS * BS]; };
+
+template <int BS>
+__device__ __forceinline__ CoefBlock<BS> load_block(const float* p) {
+  CoefBlock<BS> b;
+  if constexpr (BS == 2) {
+    const float4 x = __ldg(reinterpret_cast<const float4*>(p));
+    b.v[0] = x.x; b.v[1] = x.y; b.v[2] = x.z; b.v[3] = x.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < BS * BS; ++k) b.v[k] = __ldg(p + k);
+  }
+  return b;
+}
+
+template <int BS, int UNROLL>
+__device__ __forceinline__ void group_node(const StepArgs& a, const GroupArgs& gr, int gi,
+                                           int node, int lane) {
+  const int row0 = __ldg(gr.row0[gi] + node);
+  const int p0 = __ldg(gr.nptr[gi] + node), p1 = __ldg(gr.nptr[gi] + node + 1);
+  const int32_t* nrow = gr.nrow[gi];
+  const float* coef = gr.coef[gi];
+  const int R = a.R;
+  const float* un = static_cast<const float*>(a.u_n);
+  const float* upv = static_cast<const float*>(a.u_prev);
+  float* unew = static_cast<float*>(a.u_new);
+  for (int c = lane * 2; c < R; c += 64) {
+    const float* uc = un + c;
+    float2 uo[BS], acc[BS];
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      uo[k] = __ldg(reinterpret_cast<const float2*>(uc + (size_t)(row0 + k) * R));
+      acc[k] = make_float2(0.f, 0.f);
+    }
+    for (int e0 = p0; e0 < p1; e0 += UNROLL) {
+      float2 g[UNROLL][BS];
+      int rb[UNROLL];
+#pragma unroll
+      for (int t = 0; t < UNROLL; ++t) rb[t] = (e0 + t < p1) ? __ldg(nrow + e0 + t) : row0;
+#pragma unroll
+      for (int t = 0; t < UNROLL; ++t)
+#pragma unroll
+        for (int l = 0; l < BS; ++l)
+          g[t][l] = __ldg(reinterpret_cast<const float2*>(uc + (size_t)(rb[t] + l) * R));
+#pragma unroll
+      for (int t = 0; t < UNROLL; ++t) {
+        if (e0 + t < p1) {
+          const CoefBlock<BS> cb = load_block<BS>(coef + (size_t)(e0 + t) * (BS * BS));
+#pragma unroll
+          for (int l = 0; l < BS; ++l) {
+            const float dx = g[t][l].x - uo[l].x, dy = g[t][l].y - uo[l].y;
+#pragma unroll
+            for (int k = 0; k < BS; ++k) {
+              acc[k].x = fmaf(cb.v[k * BS + l], dx, acc[k].x);
+              acc[k].y = fmaf(cb.v[k * BS + l], dy, acc[k].y);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      const int row = row0 + k;
+      const uint32_t info = __ldg(a.rowinfo + row);
+      const float q = __ldg(static_cast<const float*>(a.rowc) + row);
+      const size_t o = (size_t)row * R + c;
+      const float2 up = __ldcs(reinterpret_cast<const float2*>(upv + o));
+      const float uiv[2] = {uo[k].x, uo[k].y};
+      const float upvv[2] = {up.x, up.y};
+      const float accv[2] = {acc[k].x, acc[k].y};
+      float res[2], vint[2];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        float dd, err;
+        two_sum(uiv[v], -upvv[v], dd, err);
+        float inc = fmaf(q, dd, -accv[v]);
+        if (info & kRowForced) inc += forcing_sum<float>(a, row, c + v);
+        inc = fmaf(q, err, inc);
+        res[v] = uiv[v] + inc;
+        vint[v] = a.int_base_prev ? (dd + err + inc) : (dd + err);
+      }
+      *reinterpret_cast<float2*>(unew + o) = make_float2(res[0], res[1]);
+      if (info & kRowInterface) {
+        const int t = lower_bound_i32(a.int_row, a.n_int, row);
+        *reinterpret_cast<float2*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) =
+            make_float2(vint[0], vint[1]);
+      } else if (info & kRowMonitored) {
+        write_history(a, row, c, (double)res[0]);
+        write_history(a, row, c + 1, (double)res[1]);
+      }
+    }
+  }
+}
+
+template <int UNROLL>
+__global__ void __launch_bounds__(256) step_f32_group(StepArgs a, GroupArgs gr) {
+  const int lane = threadIdx.x & 31;
+  const int b = blockIdx.x;
+  int gi = 0;
+#pragma unroll
+  for (int k = 1; k < kMaxGroups; ++k)
+    if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
+  const int node = (b - gr.blk_begin[gi]) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (node >= gr.n_nodes[gi]) return;
+  switch (gr.bs[gi]) {
+    case 1: group_node<1, UNROLL * 2>(a, gr, gi, node, lane); break;
+    case 2: group_node<2, UNROLL>(a, gr, gi, node, lane); break;
+    default: group_node<3, UNROLL>(a, gr, gi, node, lane); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
 template <typename T>
@@ -482,17 +601,23 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 // Variants for the autotuner. FP32 with R % 64 == 0: 0 = slice-staged
 // row kernel, 1..3 = half-warp float4 row kernels, 4 = node-block kernel
 // (only when the plan has node blocks), 5 = node-block kernel, deeper unroll.
-int batched_variants(int precision, int R, bool have_nodes) {
-  if (precision == 1 && R % 64 == 0) return have_nodes ? 6 : 4;
+// 6, 7 = group block-sparse kernel (unroll 2, 4), when the plan has groups.
+int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
+  if (precision == 1 && R % 64 == 0) return have_groups ? 8 : (have_nodes ? 6 : 4);
   return 1;
 }
 
-cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, int precision,
-                                int max_slice_entries, int variant, cudaStream_t st) {
+cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const GroupArgs* gr,
+                                int precision, int max_slice_entries, int variant,
+                                cudaStream_t st) {
   const int threads = 256;
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
+  } else if (a.R % 64 == 0 && (variant == 6 || variant == 7) && gr) {
+    const int grid = gr->blk_begin[gr->n_groups];
+    if (variant == 6) step_f32_group<2><<<grid, threads, 0, st>>>(a, *gr);
+    else step_f32_group<4><<<grid, threads, 0, st>>>(a, *gr);
   } else if (a.R % 64 == 0 && (variant == 4 || variant == 5) && g) {
     const int grid = (g->n_nodes + kNodeWarps - 1) / kNodeWarps;
     if (variant == 4) step_f32_node<3, 8><<<grid, kNodeWarps * 32, 0, st>>>(a, *g);

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <numeric>
@@ -241,6 +242,11 @@ struct bfe_plan {
   DevBuf<int32_t> nbr_ptr, coef_ptr;
   DevBuf<uint32_t> gword;
   DevBuf<float> coef;
+  // group block-sparse operator (FP32 difference form)
+  bool have_groups = false;
+  bfe::GroupArgs groups{};
+  DevBuf<int32_t> g_row0[bfe::kMaxGroups], g_nptr[bfe::kMaxGroups], g_nrow[bfe::kMaxGroups];
+  DevBuf<float> g_coef[bfe::kMaxGroups];
   bfe::NodeArgs node_args() const {
     bfe::NodeArgs g{};
     g.n_nodes = n_nodes;
@@ -602,6 +608,97 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
       CUDA_TRY(pl->coef.upload(hc));
     }
   }
+  // Group block-sparse form: DOF types coupled by K form groups; each group
+  // becomes a block-sparse matrix with BS x BS blocks over the nodes that
+  // carry it (requires the difference form on every row and consecutive
+  // group rows inside each node block).
+  if (precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0) {
+    std::map<int32_t, int32_t> parent;
+    for (int64_t i = 0; i < n; ++i) parent.emplace(dof_type[i], dof_type[i]);
+    std::function<int32_t(int32_t)> find = [&](int32_t x) {
+      while (parent[x] != x) x = parent[x] = parent[parent[x]];
+      return x;
+    };
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
+        const int32_t a1 = find(dof_type[i]), b1 = find(dof_type[K.idx[e]]);
+        if (a1 != b1) parent[std::max(a1, b1)] = std::min(a1, b1);
+      }
+    std::map<int32_t, std::vector<int32_t>> gtypes;   // root -> sorted types
+    for (auto& kv : parent) gtypes[find(kv.first)].push_back(kv.first);
+    bool ok = gtypes.size() <= (size_t)bfe::kMaxGroups;
+    std::vector<std::vector<int32_t>> types;
+    for (auto& kv : gtypes) { types.push_back(kv.second); if (kv.second.size() > 3) ok = false; }
+    std::map<int32_t, std::pair<int, int>> type_pos;  // type -> (group, position)
+    for (size_t gi = 0; gi < types.size(); ++gi)
+      for (size_t k = 0; k < types[gi].size(); ++k) type_pos[types[gi][k]] = {(int)gi, (int)k};
+    std::vector<std::vector<int32_t>> row0s(types.size());
+    // every node block: each group it touches must be complete and consecutive
+    for (int64_t b = 0; b < n && ok; b += blk_len[b]) {
+      for (int64_t k = b; k < b + blk_len[b]; ++k) {
+        const auto tp = type_pos[dof_type[k]];
+        if (tp.second != 0) continue;
+        const auto& ty = types[tp.first];
+        if (k + (int64_t)ty.size() > b + blk_len[b]) { ok = false; break; }
+        for (size_t l = 0; l < ty.size(); ++l)
+          if (dof_type[k + l] != ty[l]) ok = false;
+        row0s[tp.first].push_back((int32_t)k);
+      }
+      for (int64_t k = b; k < b + blk_len[b]; ++k) {
+        const auto tp = type_pos[dof_type[k]];
+        if (tp.second != 0 && (k - tp.second < b || dof_type[k - tp.second] != types[tp.first][0])) ok = false;
+      }
+    }
+    if (ok) {
+      int32_t blocks = 0;
+      pl->groups.n_groups = (int32_t)types.size();
+      for (size_t gi = 0; gi < types.size() && ok; ++gi) {
+        const int bs = (int)types[gi].size();
+        std::vector<int32_t> nptr(1, 0), nrow;
+        std::vector<float> coef;
+        std::vector<int64_t> nb_rows;
+        for (int32_t a0 : row0s[gi]) {
+          nb_rows.clear();
+          for (int k = 0; k < bs; ++k)
+            for (int64_t e = K.ptr[a0 + k]; e < K.ptr[a0 + k + 1]; ++e) {
+              const int64_t j = K.idx[e];
+              if (dof_node[j] == dof_node[a0]) continue;
+              nb_rows.push_back(j - type_pos[dof_type[j]].second);
+            }
+          std::sort(nb_rows.begin(), nb_rows.end());
+          nb_rows.erase(std::unique(nb_rows.begin(), nb_rows.end()), nb_rows.end());
+          for (int64_t b0 : nb_rows) {
+            nrow.push_back((int32_t)b0);
+            for (int k = 0; k < bs; ++k) {
+              const int64_t row = a0 + k;
+              const int64_t* beg = K.idx.data() + K.ptr[row];
+              const int64_t* end = K.idx.data() + K.ptr[row + 1];
+              for (int l = 0; l < bs; ++l) {
+                const int64_t* hit = std::lower_bound(beg, end, b0 + l);
+                coef.push_back(hit != end && *hit == b0 + l ? (float)(lscale[row] * K.val[hit - K.idx.data()]) : 0.0f);
+              }
+            }
+          }
+          nptr.push_back((int32_t)nrow.size());
+        }
+        if (coef.size() >= (size_t)INT32_MAX) { ok = false; break; }
+        pl->groups.bs[gi] = bs;
+        pl->groups.n_nodes[gi] = (int32_t)row0s[gi].size();
+        pl->groups.blk_begin[gi] = blocks;
+        blocks += (int32_t)((row0s[gi].size() + 7) / 8);
+        CUDA_TRY(pl->g_row0[gi].upload(row0s[gi]));
+        CUDA_TRY(pl->g_nptr[gi].upload(nptr));
+        CUDA_TRY(pl->g_nrow[gi].upload(nrow));
+        CUDA_TRY(pl->g_coef[gi].upload(coef));
+        pl->groups.row0[gi] = pl->g_row0[gi].p;
+        pl->groups.nptr[gi] = pl->g_nptr[gi].p;
+        pl->groups.nrow[gi] = pl->g_nrow[gi].p;
+        pl->groups.coef[gi] = pl->g_coef[gi].p;
+      }
+      pl->groups.blk_begin[pl->groups.n_groups] = blocks;
+      pl->have_groups = ok && blocks > 0;
+    }
+  }
   pl->nnz_operator = stored;
   pl->nnz_padded = (int64_t)hcol.size();
   pl->n_direct_rows = direct_rows;
@@ -763,6 +860,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   stt.n_interface = pl->n_int;
   stt.n_direct_rows = pl->n_direct_rows;
   stt.n_nodes = pl->have_node_blocks ? pl->n_nodes : 0;
+  stt.n_groups = pl->have_groups ? pl->groups.n_groups : 0;
   if (prec == BFE_PREC_SINGLE && rs.n_sig > 0) stt.aux_launches += 1;
   // optional per-launch CUDA-event timing: events are recorded around every
   // launch on the launching stream and summed after the run
@@ -786,8 +884,9 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   int variant = 0;
   const bfe::NodeArgs g = pl->node_args();
   const bfe::NodeArgs* gp = pl->have_node_blocks ? &g : nullptr;
+  const bfe::GroupArgs* grp = pl->have_groups ? &pl->groups : nullptr;
   if (R > 1) {
-    const int nv = bfe::batched_variants(prec, (int)R, pl->have_node_blocks);
+    const int nv = bfe::batched_variants(prec, (int)R, pl->have_node_blocks, pl->have_groups);
     auto it = pl->variant_of_R.find(R);
     const char* force = getenv("BFE_VARIANT");
     if (force && nv > 1) {
@@ -804,9 +903,9 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       CUDA_TRY(cudaEventCreate(&e1));
       float best = 1e30f;
       for (int v = 0; v < nv; ++v) {
-        CUDA_TRY(bfe::launch_step_batched(a, gp, prec, pl->max_slice_entries, v, st));   // warm
+        CUDA_TRY(bfe::launch_step_batched(a, gp, grp, prec, pl->max_slice_entries, v, st));   // warm
         CUDA_TRY(cudaEventRecord(e0, st));
-        for (int k = 0; k < 3; ++k) CUDA_TRY(bfe::launch_step_batched(a, gp, prec, pl->max_slice_entries, v, st));
+        for (int k = 0; k < 3; ++k) CUDA_TRY(bfe::launch_step_batched(a, gp, grp, prec, pl->max_slice_entries, v, st));
         CUDA_TRY(cudaEventRecord(e1, st));
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;
@@ -830,7 +929,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     a.u_new = U[inew];
     if (timing) CUDA_TRY(mark(ev_step));
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, gp, prec, pl->max_slice_entries, variant, st);
+                           : bfe::launch_step_batched(a, gp, grp, prec, pl->max_slice_entries, variant, st);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (timing) CUDA_TRY(mark(ev_step));
     stt.step_launches++;

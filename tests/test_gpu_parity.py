@@ -170,10 +170,11 @@ def test_errors_through_the_abi(bfe, plate):
             plan.run(t, [1, 2], np.ones((3, 20)), [1])             # 3 rows for 2 DOFs
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
     """Each kernel the autotuner can pick (forced through BFE_VARIANT) gives
-    the same answers; variants 4 and 5 are the node-block kernel."""
+    the same answers; variants 4, 5 are the node-block kernel and 6, 7 the
+    group block-sparse kernel."""
     m = coupled
     nt = 150
     t, s = modelgen.pulse(nt, m["dt"])
@@ -187,7 +188,7 @@ def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
         hb = plan.run_batched(t, srcs, s, hi)
         st = plan.stats()
     assert st["variant"] == variant
-    assert st["n_nodes"] > 0
+    assert st["n_nodes"] > 0 and st["n_groups"] == 2          # solid {1,2}, fluid {4}
     for r in (0, 33):
         h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
         assert _err(hb[:q4, :, r], h0[:q4]) <= TOL32
