@@ -546,6 +546,190 @@ __global__ void __launch_bounds__(256) step_f32_group(StepArgs a, GroupArgs gr) 
 }
 
 // ---------------------------------------------------------------------------
+// FP32 group block-sparse kernel with asynchronous staging (R a multiple of
+// 64). Each warp walks work items (node, 64-RHS chunk) of all groups with a
+// grid stride. For every item it copies, with cp.async (16 bytes per lane,
+// no registers held), the node's own BS state rows, its neighbours' BS rows
+// and its own previous-state rows into a shared-memory stage; the copies of
+// the next item are in flight while the current one is computed from shared
+// memory (double buffering, hardware wait_group, no spin loops). Items whose
+// rows do not fit a stage are computed with direct loads.
+constexpr int kAsyncWarps = 8;
+constexpr int kStageRows = 24;
+constexpr int kRowFloats = 64;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+struct Item {
+  int gi, node, c;     // group, node in group, first RHS of the 64-chunk
+  int bs, row0, p0, nn;
+  bool fits;
+};
+
+__device__ __forceinline__ Item make_item(const StepArgs& a, const GroupArgs& gr, long v) {
+  Item it;
+  const int chunks = a.R / 64;
+  long node_all = v / chunks;
+  it.c = (int)(v % chunks) * 64;
+  int gi = 0;
+  while (gi + 1 < gr.n_groups && node_all >= gr.n_nodes[gi]) { node_all -= gr.n_nodes[gi]; ++gi; }
+  it.gi = gi;
+  it.node = (int)node_all;
+  it.bs = gr.bs[gi];
+  it.row0 = __ldg(gr.row0[gi] + it.node);
+  it.p0 = __ldg(gr.nptr[gi] + it.node);
+  it.nn = __ldg(gr.nptr[gi] + it.node + 1) - it.p0;
+  it.fits = it.bs * (it.nn + 2) <= kStageRows;
+  return it;
+}
+
+// Issue the copies of one item: rows [0, bs) own u_n, [bs, bs(1+nn)) the
+// neighbour blocks, [bs(1+nn), bs(2+nn)) own u_prev.
+__device__ __forceinline__ void issue_item(const StepArgs& a, const GroupArgs& gr, const Item& it,
+                                           float* stage, int lane) {
+  if (!it.fits) return;
+  const int R = a.R;
+  const float* un = static_cast<const float*>(a.u_n) + it.c;
+  const float* upv = static_cast<const float*>(a.u_prev) + it.c;
+  const int rows = it.bs * (it.nn + 2);
+  for (int ch = lane; ch < rows * 16; ch += 32) {
+    const int ri = ch >> 4, part = ch & 15;
+    const float* src;
+    if (ri < it.bs) src = un + (size_t)(it.row0 + ri) * R;
+    else if (ri < it.bs * (it.nn + 1)) {
+      const int e = (ri - it.bs) / it.bs, l = (ri - it.bs) - e * it.bs;
+      src = un + (size_t)(__ldg(gr.nrow[it.gi] + it.p0 + e) + l) * R;
+    } else src = upv + (size_t)(it.row0 + ri - it.bs * (it.nn + 1)) * R;
+    cp_async16(stage + ri * kRowFloats + part * 4, src + part * 4);
+  }
+}
+
+template <int BS>
+__device__ __forceinline__ void compute_item(const StepArgs& a, const GroupArgs& gr, const Item& it,
+                                             const float* stage, int lane) {
+  const int R = a.R;
+  const int c = it.c + lane * 2;
+  const float* coef = gr.coef[it.gi] + (size_t)it.p0 * (BS * BS);
+  float2 uo[BS], acc[BS], up[BS];
+  if (it.fits) {
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      uo[k] = *reinterpret_cast<const float2*>(stage + k * kRowFloats + lane * 2);
+      up[k] = *reinterpret_cast<const float2*>(stage + (BS * (it.nn + 1) + k) * kRowFloats + lane * 2);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      uo[k] = __ldg(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_n) + (size_t)(it.row0 + k) * R + c));
+      up[k] = __ldcs(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_prev) + (size_t)(it.row0 + k) * R + c));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < BS; ++k) acc[k] = make_float2(0.f, 0.f);
+  for (int e = 0; e < it.nn; ++e) {
+    const CoefBlock<BS> cb = load_block<BS>(coef + (size_t)e * (BS * BS));
+    float2 g[BS];
+    if (it.fits) {
+#pragma unroll
+      for (int l = 0; l < BS; ++l)
+        g[l] = *reinterpret_cast<const float2*>(stage + (BS * (1 + e) + l) * kRowFloats + lane * 2);
+    } else {
+      const int rb = __ldg(gr.nrow[it.gi] + it.p0 + e);
+#pragma unroll
+      for (int l = 0; l < BS; ++l)
+        g[l] = __ldg(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_n) + (size_t)(rb + l) * R + c));
+    }
+#pragma unroll
+    for (int l = 0; l < BS; ++l) {
+      const float dx = g[l].x - uo[l].x, dy = g[l].y - uo[l].y;
+#pragma unroll
+      for (int k = 0; k < BS; ++k) {
+        acc[k].x = fmaf(cb.v[k * BS + l], dx, acc[k].x);
+        acc[k].y = fmaf(cb.v[k * BS + l], dy, acc[k].y);
+      }
+    }
+  }
+  float* unew = static_cast<float*>(a.u_new);
+#pragma unroll
+  for (int k = 0; k < BS; ++k) {
+    const int row = it.row0 + k;
+    const uint32_t info = __ldg(a.rowinfo + row);
+    const float q = __ldg(static_cast<const float*>(a.rowc) + row);
+    const size_t o = (size_t)row * R + c;
+    const float uiv[2] = {uo[k].x, uo[k].y};
+    const float upvv[2] = {up[k].x, up[k].y};
+    const float accv[2] = {acc[k].x, acc[k].y};
+    float res[2], vint[2];
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      float dd, err;
+      two_sum(uiv[v], -upvv[v], dd, err);
+      float inc = fmaf(q, dd, -accv[v]);
+      if (info & kRowForced) inc += forcing_sum<float>(a, row, c + v);
+      inc = fmaf(q, err, inc);
+      res[v] = uiv[v] + inc;
+      vint[v] = a.int_base_prev ? (dd + err + inc) : (dd + err);
+    }
+    *reinterpret_cast<float2*>(unew + o) = make_float2(res[0], res[1]);
+    if (info & kRowInterface) {
+      const int t = lower_bound_i32(a.int_row, a.n_int, row);
+      *reinterpret_cast<float2*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) =
+          make_float2(vint[0], vint[1]);
+    } else if (info & kRowMonitored) {
+      write_history(a, row, c, (double)res[0]);
+      write_history(a, row, c + 1, (double)res[1]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kAsyncWarps * 32, 2) step_f32_group_async(StepArgs a, GroupArgs gr, long n_items) {
+  extern __shared__ __align__(16) float smem_stage[];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  float* st0 = smem_stage + (size_t)wid * 2 * kStageRows * kRowFloats;
+  float* st1 = st0 + kStageRows * kRowFloats;
+  const long stride = (long)gridDim.x * kAsyncWarps;
+  long v = (long)blockIdx.x * kAsyncWarps + wid;
+  if (v >= n_items) return;
+  Item cur = make_item(a, gr, v);
+  issue_item(a, gr, cur, st0, lane);
+  cp_async_commit();
+  int buf = 0;
+  while (true) {
+    const long vn = v + stride;
+    Item nxt;
+    const bool has_next = vn < n_items;
+    if (has_next) {
+      nxt = make_item(a, gr, vn);
+      issue_item(a, gr, nxt, buf ? st0 : st1, lane);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    const float* stg = buf ? st1 : st0;
+    switch (cur.bs) {
+      case 1: compute_item<1>(a, gr, cur, stg, lane); break;
+      case 2: compute_item<2>(a, gr, cur, stg, lane); break;
+      default: compute_item<3>(a, gr, cur, stg, lane); break;
+    }
+    __syncwarp();
+    if (!has_next) break;
+    cur = nxt;
+    v = vn;
+    buf ^= 1;
+  }
+  cp_async_wait<0>();
+}
+
+size_t async_smem_bytes() { return (size_t)kAsyncWarps * 2 * kStageRows * kRowFloats * sizeof(float); }
+
+// ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
 template <typename T>
@@ -601,9 +785,10 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 // Variants for the autotuner. FP32 with R % 64 == 0: 0 = slice-staged
 // row kernel, 1..3 = half-warp float4 row kernels, 4 = node-block kernel
 // (only when the plan has node blocks), 5 = node-block kernel, deeper unroll.
-// 6, 7 = group block-sparse kernel (unroll 2, 4), when the plan has groups.
+// 6, 7 = group block-sparse kernel (unroll 2, 4), 8 = group block-sparse
+// kernel with cp.async double-buffered staging, when the plan has groups.
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
-  if (precision == 1 && R % 64 == 0) return have_groups ? 8 : (have_nodes ? 6 : 4);
+  if (precision == 1 && R % 64 == 0) return have_groups ? 9 : (have_nodes ? 6 : 4);
   return 1;
 }
 
@@ -614,6 +799,19 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
+  } else if (a.R % 64 == 0 && variant == 8 && gr) {
+    static int sm_count = 0;
+    if (sm_count == 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+      cudaFuncSetAttribute(step_f32_group_async, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)async_smem_bytes());
+    }
+    long n_items = 0;
+    for (int k = 0; k < gr->n_groups; ++k) n_items += gr->n_nodes[k];
+    n_items *= a.R / 64;
+    step_f32_group_async<<<sm_count * 2, kAsyncWarps * 32, async_smem_bytes(), st>>>(a, *gr, n_items);
   } else if (a.R % 64 == 0 && (variant == 6 || variant == 7) && gr) {
     const int grid = gr->blk_begin[gr->n_groups];
     if (variant == 6) step_f32_group<2><<<grid, threads, 0, st>>>(a, *gr);
