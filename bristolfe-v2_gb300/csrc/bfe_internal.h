@@ -101,6 +101,7 @@ struct GroupArgs {
   const int32_t* nptr[kMaxGroups];   // neighbour list of each node (n_nodes + 1)
   const int32_t* nrow[kMaxGroups];   // first row of each neighbour block
   const float* coef[kMaxGroups];     // BS*BS per neighbour block, [own k][neighbour l]
+  const int32_t* frow[kMaxGroups];   // flat neighbour rows: BS rows per neighbour block
 };
 
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.

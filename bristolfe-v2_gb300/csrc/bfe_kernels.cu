@@ -548,66 +548,85 @@ __global__ void __launch_bounds__(256) step_f32_group(StepArgs a, GroupArgs gr) 
 // ---------------------------------------------------------------------------
 // FP32 group block-sparse kernel with asynchronous staging (R a multiple of
 // 64). Each warp walks work items (node, 64-RHS chunk) of all groups with a
-// grid stride. For every item it copies, with cp.async (16 bytes per lane,
-// no registers held), the node's own BS state rows, its neighbours' BS rows
-// and its own previous-state rows into a shared-memory stage; the copies of
-// the next item are in flight while the current one is computed from shared
-// memory (double buffering, hardware wait_group, no spin loops). Items whose
-// rows do not fit a stage are computed with direct loads.
+// grid stride. For an item it copies with cp.async - two 256-byte state rows
+// per warp instruction, no registers held while in flight - the node's own
+// u_n rows, its neighbours' rows (a precomputed flat row list, read with one
+// coalesced load and distributed by shuffles), its own u_prev rows, its
+// coefficient blocks and its per-row scalars into a shared-memory stage. The
+// next item's copies are in flight while the current item is computed from
+// shared memory (double buffering, hardware wait_group, no spin loops).
+// Items that do not fit a stage are computed with direct loads.
 constexpr int kAsyncWarps = 8;
-constexpr int kStageRows = 24;
+constexpr int kStageRows = 24;      // state rows per stage
+constexpr int kStageCoef = 128;     // coefficients per stage
 constexpr int kRowFloats = 64;
+constexpr int kStageFloats = kStageRows * kRowFloats + kStageCoef + 16;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 struct Item {
-  int gi, node, c;     // group, node in group, first RHS of the 64-chunk
-  int bs, row0, p0, nn;
+  int gi, c, bs, row0, p0, nn, frow0;
   bool fits;
 };
 
 __device__ __forceinline__ Item make_item(const StepArgs& a, const GroupArgs& gr, long v) {
   Item it;
-  const int chunks = a.R / 64;
-  long node_all = v / chunks;
-  it.c = (int)(v % chunks) * 64;
+  const int chunks = a.R >> 6;
+  long node = v / chunks;
+  it.c = (int)(v - node * chunks) * 64;
   int gi = 0;
-  while (gi + 1 < gr.n_groups && node_all >= gr.n_nodes[gi]) { node_all -= gr.n_nodes[gi]; ++gi; }
+  while (gi + 1 < gr.n_groups && node >= gr.n_nodes[gi]) { node -= gr.n_nodes[gi]; ++gi; }
   it.gi = gi;
-  it.node = (int)node_all;
   it.bs = gr.bs[gi];
-  it.row0 = __ldg(gr.row0[gi] + it.node);
-  it.p0 = __ldg(gr.nptr[gi] + it.node);
-  it.nn = __ldg(gr.nptr[gi] + it.node + 1) - it.p0;
-  it.fits = it.bs * (it.nn + 2) <= kStageRows;
+  it.row0 = __ldg(gr.row0[gi] + node);
+  it.p0 = __ldg(gr.nptr[gi] + node);
+  it.nn = __ldg(gr.nptr[gi] + node + 1) - it.p0;
+  it.frow0 = it.p0 * it.bs;                // flat neighbour rows start
+  it.fits = it.bs * (it.nn + 2) <= kStageRows && it.nn * it.bs * it.bs <= kStageCoef &&
+            it.nn * it.bs <= 32;
   return it;
 }
 
-// Issue the copies of one item: rows [0, bs) own u_n, [bs, bs(1+nn)) the
-// neighbour blocks, [bs(1+nn), bs(2+nn)) own u_prev.
 __device__ __forceinline__ void issue_item(const StepArgs& a, const GroupArgs& gr, const Item& it,
                                            float* stage, int lane) {
   if (!it.fits) return;
   const int R = a.R;
   const float* un = static_cast<const float*>(a.u_n) + it.c;
   const float* upv = static_cast<const float*>(a.u_prev) + it.c;
-  const int rows = it.bs * (it.nn + 2);
-  for (int ch = lane; ch < rows * 16; ch += 32) {
-    const int ri = ch >> 4, part = ch & 15;
-    const float* src;
-    if (ri < it.bs) src = un + (size_t)(it.row0 + ri) * R;
-    else if (ri < it.bs * (it.nn + 1)) {
-      const int e = (ri - it.bs) / it.bs, l = (ri - it.bs) - e * it.bs;
-      src = un + (size_t)(__ldg(gr.nrow[it.gi] + it.p0 + e) + l) * R;
-    } else src = upv + (size_t)(it.row0 + ri - it.bs * (it.nn + 1)) * R;
-    cp_async16(stage + ri * kRowFloats + part * 4, src + part * 4);
+  const int nf = it.nn * it.bs;                       // neighbour rows
+  const int fr = lane < nf ? __ldg(gr.frow[it.gi] + it.frow0 + lane) : 0;
+  const int total = it.bs * (it.nn + 2);
+  const int half = lane >> 4, part = lane & 15;
+  for (int m2 = 0; m2 < (total + 1) >> 1; ++m2) {
+    const int m = 2 * m2 + half;
+    const int k = m - it.bs;
+    const int nbr_row = __shfl_sync(0xffffffffu, fr, k < 0 ? 0 : (k > 31 ? 31 : k));
+    if (m < total) {
+      const float* src;
+      if (m < it.bs) src = un + (size_t)(it.row0 + m) * R;
+      else if (k < nf) src = un + (size_t)nbr_row * R;
+      else src = upv + (size_t)(it.row0 + (k - nf)) * R;
+      cp_async16(stage + m * kRowFloats + part * 4, src + part * 4);
+    }
   }
+  const int ncoef = nf * it.bs;
+  const float* cf = gr.coef[it.gi] + (size_t)it.p0 * it.bs * it.bs;
+  float* sc = stage + kStageRows * kRowFloats;
+  for (int e = lane; e < ncoef; e += 32) cp_async4(sc + e, cf + e);
+  float* sm = sc + kStageCoef;
+  if (lane < it.bs) cp_async4(sm + lane, a.rowinfo + it.row0 + lane);
+  else if (lane >= 8 && lane < 8 + it.bs)
+    cp_async4(sm + lane, static_cast<const float*>(a.rowc) + it.row0 + (lane - 8));
 }
 
 template <int BS>
@@ -615,43 +634,55 @@ __device__ __forceinline__ void compute_item(const StepArgs& a, const GroupArgs&
                                              const float* stage, int lane) {
   const int R = a.R;
   const int c = it.c + lane * 2;
-  const float* coef = gr.coef[it.gi] + (size_t)it.p0 * (BS * BS);
+  const float* sc = stage + kStageRows * kRowFloats;
+  const float* sm = sc + kStageCoef;
   float2 uo[BS], acc[BS], up[BS];
+  uint32_t info[BS];
+  float qv[BS];
   if (it.fits) {
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
       uo[k] = *reinterpret_cast<const float2*>(stage + k * kRowFloats + lane * 2);
       up[k] = *reinterpret_cast<const float2*>(stage + (BS * (it.nn + 1) + k) * kRowFloats + lane * 2);
+      info[k] = reinterpret_cast<const uint32_t*>(sm)[k];
+      qv[k] = sm[8 + k];
     }
   } else {
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
       uo[k] = __ldg(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_n) + (size_t)(it.row0 + k) * R + c));
       up[k] = __ldcs(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_prev) + (size_t)(it.row0 + k) * R + c));
+      info[k] = __ldg(a.rowinfo + it.row0 + k);
+      qv[k] = __ldg(static_cast<const float*>(a.rowc) + it.row0 + k);
     }
   }
 #pragma unroll
   for (int k = 0; k < BS; ++k) acc[k] = make_float2(0.f, 0.f);
+  const float* cg = gr.coef[it.gi] + (size_t)it.p0 * (BS * BS);
   for (int e = 0; e < it.nn; ++e) {
-    const CoefBlock<BS> cb = load_block<BS>(coef + (size_t)e * (BS * BS));
     float2 g[BS];
+    float cv[BS * BS];
     if (it.fits) {
 #pragma unroll
       for (int l = 0; l < BS; ++l)
         g[l] = *reinterpret_cast<const float2*>(stage + (BS * (1 + e) + l) * kRowFloats + lane * 2);
+#pragma unroll
+      for (int t = 0; t < BS * BS; ++t) cv[t] = sc[e * BS * BS + t];
     } else {
-      const int rb = __ldg(gr.nrow[it.gi] + it.p0 + e);
 #pragma unroll
       for (int l = 0; l < BS; ++l)
-        g[l] = __ldg(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_n) + (size_t)(rb + l) * R + c));
+        g[l] = __ldg(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_n) +
+                                                     (size_t)__ldg(gr.frow[it.gi] + it.frow0 + e * BS + l) * R + c));
+#pragma unroll
+      for (int t = 0; t < BS * BS; ++t) cv[t] = __ldg(cg + e * BS * BS + t);
     }
 #pragma unroll
     for (int l = 0; l < BS; ++l) {
       const float dx = g[l].x - uo[l].x, dy = g[l].y - uo[l].y;
 #pragma unroll
       for (int k = 0; k < BS; ++k) {
-        acc[k].x = fmaf(cb.v[k * BS + l], dx, acc[k].x);
-        acc[k].y = fmaf(cb.v[k * BS + l], dy, acc[k].y);
+        acc[k].x = fmaf(cv[k * BS + l], dx, acc[k].x);
+        acc[k].y = fmaf(cv[k * BS + l], dy, acc[k].y);
       }
     }
   }
@@ -659,8 +690,6 @@ __device__ __forceinline__ void compute_item(const StepArgs& a, const GroupArgs&
 #pragma unroll
   for (int k = 0; k < BS; ++k) {
     const int row = it.row0 + k;
-    const uint32_t info = __ldg(a.rowinfo + row);
-    const float q = __ldg(static_cast<const float*>(a.rowc) + row);
     const size_t o = (size_t)row * R + c;
     const float uiv[2] = {uo[k].x, uo[k].y};
     const float upvv[2] = {up[k].x, up[k].y};
@@ -670,18 +699,18 @@ __device__ __forceinline__ void compute_item(const StepArgs& a, const GroupArgs&
     for (int v = 0; v < 2; ++v) {
       float dd, err;
       two_sum(uiv[v], -upvv[v], dd, err);
-      float inc = fmaf(q, dd, -accv[v]);
-      if (info & kRowForced) inc += forcing_sum<float>(a, row, c + v);
-      inc = fmaf(q, err, inc);
+      float inc = fmaf(qv[k], dd, -accv[v]);
+      if (info[k] & kRowForced) inc += forcing_sum<float>(a, row, c + v);
+      inc = fmaf(qv[k], err, inc);
       res[v] = uiv[v] + inc;
       vint[v] = a.int_base_prev ? (dd + err + inc) : (dd + err);
     }
     *reinterpret_cast<float2*>(unew + o) = make_float2(res[0], res[1]);
-    if (info & kRowInterface) {
+    if (info[k] & kRowInterface) {
       const int t = lower_bound_i32(a.int_row, a.n_int, row);
       *reinterpret_cast<float2*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) =
           make_float2(vint[0], vint[1]);
-    } else if (info & kRowMonitored) {
+    } else if (info[k] & kRowMonitored) {
       write_history(a, row, c, (double)res[0]);
       write_history(a, row, c + 1, (double)res[1]);
     }
@@ -692,8 +721,8 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, 2) step_f32_group_async(Step
   extern __shared__ __align__(16) float smem_stage[];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
-  float* st0 = smem_stage + (size_t)wid * 2 * kStageRows * kRowFloats;
-  float* st1 = st0 + kStageRows * kRowFloats;
+  float* st0 = smem_stage + (size_t)wid * 2 * kStageFloats;
+  float* st1 = st0 + kStageFloats;
   const long stride = (long)gridDim.x * kAsyncWarps;
   long v = (long)blockIdx.x * kAsyncWarps + wid;
   if (v >= n_items) return;
@@ -727,7 +756,7 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, 2) step_f32_group_async(Step
   cp_async_wait<0>();
 }
 
-size_t async_smem_bytes() { return (size_t)kAsyncWarps * 2 * kStageRows * kRowFloats * sizeof(float); }
+size_t async_smem_bytes() { return (size_t)kAsyncWarps * 2 * kStageFloats * sizeof(float); }
 
 // ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread

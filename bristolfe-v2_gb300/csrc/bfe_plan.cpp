@@ -246,6 +246,7 @@ struct bfe_plan {
   bool have_groups = false;
   bfe::GroupArgs groups{};
   DevBuf<int32_t> g_row0[bfe::kMaxGroups], g_nptr[bfe::kMaxGroups], g_nrow[bfe::kMaxGroups];
+  DevBuf<int32_t> g_frow[bfe::kMaxGroups];
   DevBuf<float> g_coef[bfe::kMaxGroups];
   bfe::NodeArgs node_args() const {
     bfe::NodeArgs g{};
@@ -690,6 +691,12 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         CUDA_TRY(pl->g_nptr[gi].upload(nptr));
         CUDA_TRY(pl->g_nrow[gi].upload(nrow));
         CUDA_TRY(pl->g_coef[gi].upload(coef));
+        std::vector<int32_t> frow;
+        frow.reserve(nrow.size() * bs);
+        for (int32_t r0 : nrow)
+          for (int l = 0; l < bs; ++l) frow.push_back(r0 + l);
+        CUDA_TRY(pl->g_frow[gi].upload(frow));
+        pl->groups.frow[gi] = pl->g_frow[gi].p;
         pl->groups.row0[gi] = pl->g_row0[gi].p;
         pl->groups.nptr[gi] = pl->g_nptr[gi].p;
         pl->groups.nrow[gi] = pl->g_nrow[gi].p;
