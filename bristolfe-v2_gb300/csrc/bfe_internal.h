@@ -102,6 +102,7 @@ struct GroupArgs {
   const int32_t* nrow[kMaxGroups];   // first row of each neighbour block
   const float* coef[kMaxGroups];     // BS*BS per neighbour block, [own k][neighbour l]
   const int32_t* frow[kMaxGroups];   // flat neighbour rows: BS rows per neighbour block
+  const float2* coef2[kMaxGroups];   // the coefficients as broadcast pairs {c, c}
 };
 
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.

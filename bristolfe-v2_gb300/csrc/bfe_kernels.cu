@@ -759,6 +759,99 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, 2) step_f32_group_async(Step
 size_t async_smem_bytes() { return (size_t)kAsyncWarps * 2 * kStageFloats * sizeof(float); }
 
 // ---------------------------------------------------------------------------
+// FP32 group block-sparse kernel, packed-math form (R a multiple of 64).
+// One warp per node of a group, each lane owns two right-hand sides held as
+// a float2 and every arithmetic operation is one packed FP32x2 instruction
+// (__ffma2_rn / __fadd2_rn: IEEE round-to-nearest per component, the same
+// results as two scalar operations). Coefficients are stored as pre-broadcast
+// float2 pairs ({c, c}). The neighbour differences are formed as
+// (u_own - u_nbr), so the accumulator holds -Lp u and the compensated update
+// needs no negation.
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {        // a - b, exact rounding
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = f2sub(s, a);
+  e = __fadd2_rn(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
+}
+
+template <int BS, int UNROLL>
+__device__ __forceinline__ void group2_node(const StepArgs& a, const GroupArgs& gr, int gi,
+                                            int node, int lane) {
+  const int row0 = __ldg(gr.row0[gi] + node);
+  const int p0 = __ldg(gr.nptr[gi] + node), p1 = __ldg(gr.nptr[gi] + node + 1);
+  const int32_t* nrow = gr.nrow[gi];
+  const float2* coef = gr.coef2[gi];
+  const int R = a.R;
+  const size_t rstride = (size_t)R * sizeof(float);
+  for (int c = lane * 2; c < R; c += 64) {
+    const char* ub = reinterpret_cast<const char*>(static_cast<const float*>(a.u_n) + c);
+    float2 uo[BS], acc[BS];
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      uo[k] = __ldg(reinterpret_cast<const float2*>(ub + (size_t)(row0 + k) * rstride));
+      acc[k] = make_float2(0.f, 0.f);
+    }
+#pragma unroll UNROLL
+    for (int e = p0; e < p1; ++e) {
+      const char* nb = ub + (size_t)__ldg(nrow + e) * rstride;
+      const float2* cb = coef + (size_t)e * (BS * BS);
+#pragma unroll
+      for (int l = 0; l < BS; ++l) {
+        const float2 g = __ldg(reinterpret_cast<const float2*>(nb + l * rstride));
+        const float2 dn = f2sub(uo[l], g);                      // u_own - u_nbr
+#pragma unroll
+        for (int k = 0; k < BS; ++k) acc[k] = __ffma2_rn(__ldg(cb + k * BS + l), dn, acc[k]);
+      }
+    }
+    float* unew = static_cast<float*>(a.u_new);
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      const int row = row0 + k;
+      const uint32_t info = __ldg(a.rowinfo + row);
+      const float q = __ldg(static_cast<const float*>(a.rowc) + row);
+      const size_t o = (size_t)row * R + c;
+      const float2 up = __ldcs(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_prev) + o));
+      float2 d, err;
+      two_sum2(uo[k], make_float2(-up.x, -up.y), d, err);
+      const float2 q2 = make_float2(q, q);
+      float2 inc = __ffma2_rn(q2, d, acc[k]);                    // q d - Lp u
+      if (info & kRowForced)
+        inc = __fadd2_rn(inc, make_float2(forcing_sum<float>(a, row, c), forcing_sum<float>(a, row, c + 1)));
+      inc = __ffma2_rn(q2, err, inc);
+      const float2 r = __fadd2_rn(uo[k], inc);
+      *reinterpret_cast<float2*>(unew + o) = r;
+      if (info & kRowInterface) {
+        const int t = lower_bound_i32(a.int_row, a.n_int, row);
+        const float2 vi = a.int_base_prev ? __fadd2_rn(__fadd2_rn(d, err), inc) : __fadd2_rn(d, err);
+        *reinterpret_cast<float2*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) = vi;
+      } else if (info & kRowMonitored) {
+        write_history(a, row, c, (double)r.x);
+        write_history(a, row, c + 1, (double)r.y);
+      }
+    }
+  }
+}
+
+template <int UNROLL>
+__global__ void __launch_bounds__(256) step_f32_group2(StepArgs a, GroupArgs gr) {
+  const int lane = threadIdx.x & 31;
+  const int b = blockIdx.x;
+  int gi = 0;
+#pragma unroll
+  for (int k = 1; k < kMaxGroups; ++k)
+    if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
+  const int node = (b - gr.blk_begin[gi]) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (node >= gr.n_nodes[gi]) return;
+  switch (gr.bs[gi]) {
+    case 1: group2_node<1, UNROLL * 2>(a, gr, gi, node, lane); break;
+    case 2: group2_node<2, UNROLL>(a, gr, gi, node, lane); break;
+    default: group2_node<3, UNROLL>(a, gr, gi, node, lane); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
 template <typename T>
@@ -816,8 +909,9 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 // (only when the plan has node blocks), 5 = node-block kernel, deeper unroll.
 // 6, 7 = group block-sparse kernel (unroll 2, 4), 8 = group block-sparse
 // kernel with cp.async double-buffered staging, when the plan has groups.
+// 9, 10, 11 = packed-math group kernel (unroll 1, 2, 4).
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
-  if (precision == 1 && R % 64 == 0) return have_groups ? 9 : (have_nodes ? 6 : 4);
+  if (precision == 1 && R % 64 == 0) return have_groups ? 12 : (have_nodes ? 6 : 4);
   return 1;
 }
 
@@ -828,6 +922,11 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
+  } else if (a.R % 64 == 0 && variant >= 9 && variant <= 11 && gr) {
+    const int grid = gr->blk_begin[gr->n_groups];
+    if (variant == 9) step_f32_group2<1><<<grid, threads, 0, st>>>(a, *gr);
+    else if (variant == 10) step_f32_group2<2><<<grid, threads, 0, st>>>(a, *gr);
+    else step_f32_group2<4><<<grid, threads, 0, st>>>(a, *gr);
   } else if (a.R % 64 == 0 && variant == 8 && gr) {
     static int sm_count = 0;
     if (sm_count == 0) {

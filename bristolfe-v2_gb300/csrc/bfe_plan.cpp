@@ -247,6 +247,7 @@ struct bfe_plan {
   bfe::GroupArgs groups{};
   DevBuf<int32_t> g_row0[bfe::kMaxGroups], g_nptr[bfe::kMaxGroups], g_nrow[bfe::kMaxGroups];
   DevBuf<int32_t> g_frow[bfe::kMaxGroups];
+  DevBuf<float2> g_coef2[bfe::kMaxGroups];
   DevBuf<float> g_coef[bfe::kMaxGroups];
   bfe::NodeArgs node_args() const {
     bfe::NodeArgs g{};
@@ -697,6 +698,10 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
           for (int l = 0; l < bs; ++l) frow.push_back(r0 + l);
         CUDA_TRY(pl->g_frow[gi].upload(frow));
         pl->groups.frow[gi] = pl->g_frow[gi].p;
+        std::vector<float2> coef2(coef.size());
+        for (size_t k = 0; k < coef.size(); ++k) coef2[k] = make_float2(coef[k], coef[k]);
+        CUDA_TRY(pl->g_coef2[gi].upload(coef2));
+        pl->groups.coef2[gi] = pl->g_coef2[gi].p;
         pl->groups.row0[gi] = pl->g_row0[gi].p;
         pl->groups.nptr[gi] = pl->g_nptr[gi].p;
         pl->groups.nrow[gi] = pl->g_nrow[gi].p;
