@@ -834,8 +834,8 @@ __device__ __forceinline__ void group2_node(const StepArgs& a, const GroupArgs& 
   }
 }
 
-template <int UNROLL>
-__global__ void __launch_bounds__(256) step_f32_group2(StepArgs a, GroupArgs gr) {
+template <int MAXBS, int UNROLL, int MINB>
+__global__ void __launch_bounds__(256, MINB) step_f32_group2(StepArgs a, GroupArgs gr) {
   const int lane = threadIdx.x & 31;
   const int b = blockIdx.x;
   int gi = 0;
@@ -844,11 +844,9 @@ __global__ void __launch_bounds__(256) step_f32_group2(StepArgs a, GroupArgs gr)
     if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
   const int node = (b - gr.blk_begin[gi]) * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (node >= gr.n_nodes[gi]) return;
-  switch (gr.bs[gi]) {
-    case 1: group2_node<1, UNROLL * 2>(a, gr, gi, node, lane); break;
-    case 2: group2_node<2, UNROLL>(a, gr, gi, node, lane); break;
-    default: group2_node<3, UNROLL>(a, gr, gi, node, lane); break;
-  }
+  if (gr.bs[gi] == 1) group2_node<1, UNROLL * 2>(a, gr, gi, node, lane);
+  else if (MAXBS == 2 || gr.bs[gi] == 2) group2_node<(MAXBS >= 2 ? 2 : 1), UNROLL>(a, gr, gi, node, lane);
+  else group2_node<MAXBS, UNROLL>(a, gr, gi, node, lane);
 }
 
 // ---------------------------------------------------------------------------
@@ -909,10 +907,24 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 // (only when the plan has node blocks), 5 = node-block kernel, deeper unroll.
 // 6, 7 = group block-sparse kernel (unroll 2, 4), 8 = group block-sparse
 // kernel with cp.async double-buffered staging, when the plan has groups.
-// 9, 10, 11 = packed-math group kernel (unroll 1, 2, 4).
+// 9, 10, 11 = packed-math group kernel (unroll 1, 2, 4), 12-14 = the same
+// with occupancy hints of 4, 6 and 8 resident CTAs.
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
-  if (precision == 1 && R % 64 == 0) return have_groups ? 12 : (have_nodes ? 6 : 4);
+  if (precision == 1 && R % 64 == 0) return have_groups ? 15 : (have_nodes ? 6 : 4);
   return 1;
+}
+
+template <int MAXBS>
+static void launch_group2(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {
+  const int grid = gr.blk_begin[gr.n_groups];
+  switch (variant) {
+    case 9: step_f32_group2<MAXBS, 1, 1><<<grid, 256, 0, st>>>(a, gr); break;
+    case 10: step_f32_group2<MAXBS, 2, 1><<<grid, 256, 0, st>>>(a, gr); break;
+    case 11: step_f32_group2<MAXBS, 4, 1><<<grid, 256, 0, st>>>(a, gr); break;
+    case 12: step_f32_group2<MAXBS, 1, 4><<<grid, 256, 0, st>>>(a, gr); break;
+    case 13: step_f32_group2<MAXBS, 1, 6><<<grid, 256, 0, st>>>(a, gr); break;
+    default: step_f32_group2<MAXBS, 1, 8><<<grid, 256, 0, st>>>(a, gr); break;
+  }
 }
 
 cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const GroupArgs* gr,
@@ -922,11 +934,11 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
-  } else if (a.R % 64 == 0 && variant >= 9 && variant <= 11 && gr) {
-    const int grid = gr->blk_begin[gr->n_groups];
-    if (variant == 9) step_f32_group2<1><<<grid, threads, 0, st>>>(a, *gr);
-    else if (variant == 10) step_f32_group2<2><<<grid, threads, 0, st>>>(a, *gr);
-    else step_f32_group2<4><<<grid, threads, 0, st>>>(a, *gr);
+  } else if (a.R % 64 == 0 && variant >= 9 && variant <= 14 && gr) {
+    int maxbs = 1;
+    for (int k = 0; k < gr->n_groups; ++k) maxbs = gr->bs[k] > maxbs ? gr->bs[k] : maxbs;
+    if (maxbs <= 2) launch_group2<2>(a, *gr, variant, st);
+    else launch_group2<3>(a, *gr, variant, st);
   } else if (a.R % 64 == 0 && variant == 8 && gr) {
     static int sm_count = 0;
     if (sm_count == 0) {
