@@ -105,6 +105,16 @@ struct GroupArgs {
   const float2* coef2[kMaxGroups];   // the coefficients as broadcast pairs {c, c}
 };
 
+// Extra data of the TMA-staged group kernel (bfe_tma.cu): per node the
+// 16-byte-aligned offset (in float2 units) of its coefficient pairs inside a
+// padded copy of the coefficient array, and the device error flag a bounded
+// wait sets when it runs out.
+struct TmaArgs {
+  const int32_t* cofs[kMaxGroups];
+  const float2* coefp[kMaxGroups];
+  int* err;
+};
+
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.
 cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
 // Number of kernel variants the autotuner may choose from for (precision, R).
@@ -118,5 +128,11 @@ cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_
 cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t frame,
                          int field_is_vel, double dt, cudaStream_t s);
 cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
+
+size_t tma_smem_bytes();
+// tm_un / tm_up: CUtensorMap (2D FP32 [n][R], box 64 x 1) of u_n and u_{n-1}.
+cudaError_t launch_step_tma(const StepArgs& a, const GroupArgs& gr, const TmaArgs& t,
+                            const struct CUtensorMap_st* tm_un, const struct CUtensorMap_st* tm_up,
+                            cudaStream_t s);
 
 }  // namespace bfe

@@ -909,8 +909,9 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 // kernel with cp.async double-buffered staging, when the plan has groups.
 // 9, 10, 11 = packed-math group kernel (unroll 1, 2, 4), 12-14 = the same
 // with occupancy hints of 4, 6 and 8 resident CTAs.
+// 15 = TMA-staged group kernel (bfe_tma.cu; launched by the plan code).
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
-  if (precision == 1 && R % 64 == 0) return have_groups ? 15 : (have_nodes ? 6 : 4);
+  if (precision == 1 && R % 64 == 0) return have_groups ? 16 : (have_nodes ? 6 : 4);
   return 1;
 }
 

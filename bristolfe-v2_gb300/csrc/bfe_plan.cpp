@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "bfe_internal.h"
@@ -248,6 +249,10 @@ struct bfe_plan {
   DevBuf<int32_t> g_row0[bfe::kMaxGroups], g_nptr[bfe::kMaxGroups], g_nrow[bfe::kMaxGroups];
   DevBuf<int32_t> g_frow[bfe::kMaxGroups];
   DevBuf<float2> g_coef2[bfe::kMaxGroups];
+  DevBuf<int32_t> g_cofs[bfe::kMaxGroups];
+  DevBuf<float2> g_coefp[bfe::kMaxGroups];
+  DevBuf<int> d_err;
+  bfe::TmaArgs tma{};
   DevBuf<float> g_coef[bfe::kMaxGroups];
   bfe::NodeArgs node_args() const {
     bfe::NodeArgs g{};
@@ -702,6 +707,21 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         for (size_t k = 0; k < coef.size(); ++k) coef2[k] = make_float2(coef[k], coef[k]);
         CUDA_TRY(pl->g_coef2[gi].upload(coef2));
         pl->groups.coef2[gi] = pl->g_coef2[gi].p;
+        // padded copy: each node's pairs start on a 16-byte boundary
+        std::vector<int32_t> cofs;
+        std::vector<float2> coefp;
+        for (size_t a0 = 0; a0 + 1 < nptr.size(); ++a0) {
+          if (coefp.size() & 1) coefp.push_back(make_float2(0.f, 0.f));
+          cofs.push_back((int32_t)coefp.size());
+          const size_t b0 = (size_t)nptr[a0] * bs * bs, b1 = (size_t)nptr[a0 + 1] * bs * bs;
+          for (size_t k = b0; k < b1; ++k) coefp.push_back(coef2[k]);
+        }
+        if (coefp.size() & 1) coefp.push_back(make_float2(0.f, 0.f));
+        if (coefp.empty()) coefp.push_back(make_float2(0.f, 0.f));
+        CUDA_TRY(pl->g_cofs[gi].upload(cofs));
+        CUDA_TRY(pl->g_coefp[gi].upload(coefp));
+        pl->tma.cofs[gi] = pl->g_cofs[gi].p;
+        pl->tma.coefp[gi] = pl->g_coefp[gi].p;
         pl->groups.row0[gi] = pl->g_row0[gi].p;
         pl->groups.nptr[gi] = pl->g_nptr[gi].p;
         pl->groups.nrow[gi] = pl->g_nrow[gi].p;
@@ -709,6 +729,10 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
       }
       pl->groups.blk_begin[pl->groups.n_groups] = blocks;
       pl->have_groups = ok && blocks > 0;
+      if (pl->have_groups) {
+        CUDA_TRY(pl->d_err.alloc(1));
+        pl->tma.err = pl->d_err.p;
+      }
     }
   }
   pl->nnz_operator = stored;
@@ -754,6 +778,41 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
 // ---------------------------------------------------------------------------
 // Run machinery shared by bfe_run, bfe_run_batched and bfe_run_device.
 namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 2D FP32 tensor map of an [n][R] state buffer with a 64 x 1 box (one
+// 64-RHS row segment; gather4 fetches four of them).
+bool make_state_map(CUtensorMap* m, void* base, int64_t n, int64_t R) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || R % 64 != 0 || n >= (int64_t)1 << 31) return false;
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)R, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)R * sizeof(float)};
+  const cuuint32_t box[2] = {64, 1};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 
 struct ForceEntry {
   int32_t row, rhs, sig;
@@ -893,6 +952,22 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   // variant on a few steps of the real operator (state still zero, so the
   // results are discarded by the real march that follows) and keep the
   // fastest. BFE_VARIANT=<k> forces variant k (for sweeps).
+  // tensor maps of the three state buffers for the TMA-staged kernel
+  alignas(64) CUtensorMap tmaps[3];
+  bool have_tmaps = false;
+  if (pl->have_groups && prec == BFE_PREC_SINGLE && R % 64 == 0) {
+    have_tmaps = make_state_map(&tmaps[0], U[0], n, R) && make_state_map(&tmaps[1], U[1], n, R) &&
+                 make_state_map(&tmaps[2], U[2], n, R);
+    CUDA_TRY(cudaMemsetAsync(pl->d_err.p, 0, sizeof(int), st));
+  }
+  auto launch_batched = [&](const bfe::NodeArgs* gpp, const bfe::GroupArgs* grpp, int v, int ib_n,
+                            int ib_prev) -> cudaError_t {
+    if (v == 15) {
+      if (!grpp || !have_tmaps) return cudaErrorNotSupported;
+      return bfe::launch_step_tma(a, *grpp, pl->tma, &tmaps[ib_n], &tmaps[ib_prev], st);
+    }
+    return bfe::launch_step_batched(a, gpp, grpp, prec, pl->max_slice_entries, v, st);
+  };
   int variant = 0;
   const bfe::NodeArgs g = pl->node_args();
   const bfe::NodeArgs* gp = pl->have_node_blocks ? &g : nullptr;
@@ -915,9 +990,10 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       CUDA_TRY(cudaEventCreate(&e1));
       float best = 1e30f;
       for (int v = 0; v < nv; ++v) {
-        CUDA_TRY(bfe::launch_step_batched(a, gp, grp, prec, pl->max_slice_entries, v, st));   // warm
+        if (v == 15 && !have_tmaps) continue;
+        CUDA_TRY(launch_batched(gp, grp, v, 1, 0));   // warm
         CUDA_TRY(cudaEventRecord(e0, st));
-        for (int k = 0; k < 3; ++k) CUDA_TRY(bfe::launch_step_batched(a, gp, grp, prec, pl->max_slice_entries, v, st));
+        for (int k = 0; k < 3; ++k) CUDA_TRY(launch_batched(gp, grp, v, 1, 0));
         CUDA_TRY(cudaEventRecord(e1, st));
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;
@@ -940,8 +1016,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     a.u_n = U[icur];
     a.u_new = U[inew];
     if (timing) CUDA_TRY(mark(ev_step));
-    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, gp, grp, prec, pl->max_slice_entries, variant, st);
+    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st) : launch_batched(gp, grp, variant, icur, iprev);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (timing) CUDA_TRY(mark(ev_step));
     stt.step_launches++;
@@ -967,6 +1042,11 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     inew = t;
   }
   CUDA_TRY(cudaStreamSynchronize(st));
+  if (have_tmaps) {
+    int err = 0;
+    CUDA_TRY(cudaMemcpy(&err, pl->d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(BFE_ERR_CUDA, "a TMA stage wait exceeded its iteration limit");
+  }
   for (size_t k = 0; k + 1 < ev_step.size(); k += 2) {
     float ms = 0;
     CUDA_TRY(cudaEventElapsedTime(&ms, ev_step[k], ev_step[k + 1]));
