@@ -134,6 +134,31 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+KERNEL_NAMES = {
+    0: "step_batched<float,2> (slice-staged rows)", 1: "step_f32_x64<4,4>", 2: "step_f32_x64<4,3>",
+    3: "step_f32_x64<8,2>", 4: "step_f32_node<3,8>", 5: "step_f32_node<3,12>",
+    6: "step_f32_group<2>", 7: "step_f32_group<4>", 8: "step_f32_group_async",
+    9: "step_f32_group2<2,1,1>", 10: "step_f32_group2<2,2,1>", 11: "step_f32_group2<2,4,1>",
+    12: "step_f32_group2<2,1,4>", 13: "step_f32_group2<2,1,6>", 14: "step_f32_group2<2,1,8>",
+    15: "step_f32_group_tma",
+}
+
+
+def profiled_traffic(kernel, n_dof):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/step_kernel_traffic.json), scaled to n_dof rows, or None."""
+    p = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    rec = d.get(kernel)
+    if not rec:
+        return None
+    return rec["dram_bytes_per_launch"] * n_dof / rec["n_dof"]
+
+
 def algorithmic_bytes(nnz, n, R, p, q, b):
     """Bytes one time step must move (per launch of the step kernel):
     operator values + int32 columns, row pointers, two per-row coefficient
@@ -226,6 +251,8 @@ def run_ours(args):
     stk = plan32.stats()
     plan32.set_timing(False)
     step_avg_ms = stk["step_ms"] / max(stk["step_launches"], 1)
+    aux_avg_ms = stk["aux_ms"] / max(stk["aux_launches"], 1)
+    kname = KERNEL_NAMES.get(stk["variant"], "variant %d" % stk["variant"])
     nnz = K.nnz
     bytes_step = algorithmic_bytes(nnz, n, R, p_max, q, 4)
     peak, peak_kind = measured_peak_hbm()
@@ -257,6 +284,7 @@ def run_ours(args):
     st64 = plan64.stats()
     plan64.set_timing(False)
     step64_ms = st64["step_ms"] / max(st64["step_launches"], 1)
+    aux64_ms = st64["aux_ms"] / max(st64["aux_launches"], 1)
     bytes64 = algorithmic_bytes(nnz, n, 1, srcs[r_mid].size, q, 8)
     h64 = d_hist64.cpu().numpy()[0]
     err = float(np.abs(h32[r_mid] - h64).max() / np.abs(h64).max())
@@ -287,11 +315,12 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (state %.0f MB per time step)" % (3 * R * n * 4 / 1e6),
                        "parallelism": "replicas x%d" % world, "scale": args.scale},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "step_batched<float,2>", "bytes_per_launch": bytes_step,
-                         "avg_launch_ms": step_avg_ms, "peak_source": peak_kind},
+                         "frac": achieved / peak, "traffic": profiled_traffic(kname, n),
+                         "kernel": kname, "variant": stk["variant"], "bytes_per_launch": bytes_step,
+                         "avg_launch_ms": step_avg_ms, "peak_source": peak_kind,
+                         "interface_kernel_avg_ms": aux_avg_ms},
             "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_march": ms64,
-                           "step_kernel_ms": step64_ms,
+                           "step_kernel_ms": step64_ms, "interface_kernel_ms": aux64_ms,
                            "step_kernel_gbs": bytes64 / (step64_ms * 1e-3) / 1e9,
                            "speedup_fp32_batched": value / world / value64},
             "ascan_err_vs_fp64": err,
