@@ -129,6 +129,9 @@ cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t 
                          int field_is_vel, double dt, cudaStream_t s);
 cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
 
+// Message returned by bfe_last_error() on the calling thread.
+void set_last_error(const char* msg);
+
 size_t tma_smem_bytes();
 // tm_un / tm_up: CUtensorMap (2D FP32 [n][R], box 64 x 1) of u_n and u_{n-1}.
 cudaError_t launch_step_tma(const StepArgs& a, const GroupArgs& gr, const TmaArgs& t,

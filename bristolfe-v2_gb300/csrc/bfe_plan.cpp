@@ -207,6 +207,8 @@ struct DevBuf {
 
 }  // namespace
 
+void bfe::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
 struct bfe_plan {
   int64_t n = 0;
   int32_t mode = 0, prec = 0;

@@ -171,6 +171,41 @@ int bfe_plan_set_timing(bfe_plan* plan, int32_t enable);
 /* Copy the counters of the plan's last run. */
 int bfe_plan_stats(const bfe_plan* plan, bfe_stats* out);
 
+/*
+ * Allocation-free FP64 march of one source. No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: their device memory is owned by a
+ * framework allocator or a fixed pool (MATLAB gpuArray data, a serving
+ * process with a pre-reserved budget), or they must not trigger the device
+ * synchronisation that allocating or freeing implies inside a running
+ * pipeline. Nothing is allocated: the caller passes every input and output in
+ * its own device memory, and the three state vectors live in a static device
+ * array of 3 x 1,048,576 doubles (24 MiB) that each GPU loading the library
+ * keeps until the process exits. Models above 1,048,576 DOFs are rejected
+ * with BFE_ERR_ARG.
+ *
+ * The first call on a device looks the array's address up for that device
+ * (make it before any stream capture). Every call clears the state at its
+ * start; all calls share the one array, so calls that overlap on the GPU
+ * (other streams, other threads) race and must be serialised by the caller.
+ *
+ *   u_{n+1}[i] = sum_j B_ij u_n[j] + d_i u_{n-1}[i]   (+ forcing)
+ * B in CSR (d_row_ptr[n+1], d_col, d_bval; 0-based int32) and d the diagonal
+ * of D, i.e. the reference's u = A f + B u_-1 + D u_-2 with P diagonal
+ * (fn_explicit_dynamic_solver_v6.m:130-139 without fluid-solid coupling in C).
+ * Forcing: for each of n_frc entries, u[d_frc_row[e]] += d_frc_coef[e] *
+ * d_sig[ti * n_frc + e] (the coefficient is A's diagonal times any weight).
+ * History: d_hist[k + q * ti] = u[d_hist_row[k]], q x n_t column-major; the
+ * caller zeroes it (samples before ti_start are not written).
+ */
+int bfe_run_f64_noalloc(int64_t n, const int32_t* d_row_ptr, const int32_t* d_col,
+                        const double* d_bval, const double* d_dvec,
+                        int64_t n_t, int64_t ti_start,
+                        int64_t n_frc, const int32_t* d_frc_row, const double* d_frc_coef,
+                        const double* d_sig,
+                        int64_t q, const int32_t* d_hist_row, double* d_hist,
+                        void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* bfe_last_error(void);
 
