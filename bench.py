@@ -1,14 +1,16 @@
 """Benchmark of the explicit time-marching path on one GB300 (or N replicas).
 
-Headline: FP32 batched time marching (64 sources as 64 right-hand sides of one
-launch sequence) on the coupled water/steel model - 60 x 30 mm at 0.05 mm
-(1.44M triangles), ASI2D2 interface, quadratic absorbing layers, seeded void
-blob, 64-element array on the water surface - over 6,000 samples. One bench
-step = one full march of all sources. Also measured in the same run: the
-plain FP64 form on the same model (one source), the max-normalised A-scan
-error of the FP32 batched result against that FP64 run, the step kernel's
-roofline, the end-to-end call through the C ABI with host buffers, and the
-FP64 CPU restatement of the reference's time loop on the host cores.
+Headline: FP32 batched time marching of 64 sources (64 right-hand sides) on
+the coupled water/steel model - 60 x 30 mm at 0.05 mm (1.44M triangles),
+ASI2D2 interface, quadratic absorbing layers, seeded void, 64-element array on
+the water surface - together with 32 steel scatterer sub-domain models of
+50k-400k DOF (absorbers, seeded voids) in one multi-model plan, over 6,000
+samples, replayed as CUDA graphs. One bench step = one full march of all
+sources of all models. Also measured in the same run: the plain FP64 form on
+the same models (one source), the max-normalised A-scan error of the FP32
+batched result against that FP64 run, the coupled model alone, the step
+kernel's roofline, the end-to-end call through the C ABI with host buffers,
+and the FP64 CPU restatement of the reference's time loop on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -38,12 +40,14 @@ WORKLOAD = dict(W=60e-3, H_water=20e-3, H_steel=10e-3, h=0.05e-3, fc=5e6, cycles
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink the model size (testing only; 1.0 = the benchmark model)")
     ap.add_argument("--n-t", type=int, default=None)
+    ap.add_argument("--subdomains", type=int, default=32,
+                    help="steel sub-domain models marched with the coupled model (32 = benchmark)")
     return ap.parse_args()
 
 
@@ -167,11 +171,43 @@ def algorithmic_bytes(nnz, n, R, p, q, b):
     return nnz * (b + 4) + 4 * (n + 1) + 2 * n * b + 3 * R * n * b + R * (p + q) * b
 
 
+def _build_subdomain(args):
+    """Worker: one steel sub-domain model (runs in a spawned process)."""
+    import bfe_gb300.model as model
+    side, seed = args
+    m = model.steel_subdomain(side, seed=seed, n_mon=16)
+    return {k: m[k] for k in ("K", "C", "M", "gl", "dt", "src_nodes", "mon_nodes")}
+
+
+def build_workload(w, n_sub):
+    """Coupled FMC model plus n_sub steel sub-domain models (built in a spawn
+    pool before any GPU work)."""
+    from concurrent.futures import ProcessPoolExecutor
+    import multiprocessing as mp
+    from bfe_gb300 import model
+    sides = model.subdomain_sides(n_sub, h=w["h"]) * (1.0 if w.get("scale", 1.0) == 1.0 else w["scale"])
+    subs = []
+    if n_sub:
+        with ProcessPoolExecutor(max_workers=min(n_sub, os.cpu_count() or 4),
+                                 mp_context=mp.get_context("spawn")) as ex:
+            subs = list(ex.map(_build_subdomain, [(float(sd), 100 + k) for k, sd in enumerate(sides)]))
+    main = model.coupled_water_steel(W=w["W"], H_water=w["H_water"], H_steel=w["H_steel"], h=w["h"],
+                                     fc=w["fc"], blob_polygon_pts=w["blob"],
+                                     array_elements=w["n_src"], array_pitch=w["pitch"])
+    return main, subs
+
+
 def run_ours(args):
+    from bfe_gb300 import model
+    w = workload(args.scale)
+    w["scale"] = args.scale
+    n_t = args.n_t or w["n_t"]
+    t0 = time.perf_counter()
+    main, subs = build_workload(w, args.subdomains)
+    t_build = time.perf_counter() - t0
+
     import torch
     import bfe_gb300
-    from bfe_gb300 import model
-
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
@@ -181,41 +217,46 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     bfe_gb300.load()
-    w = workload(args.scale)
-    n_t = args.n_t or w["n_t"]
-    t0 = time.perf_counter()
-    m = model.coupled_water_steel(W=w["W"], H_water=w["H_water"], H_steel=w["H_steel"], h=w["h"],
-                                  fc=w["fc"], blob_polygon_pts=w["blob"],
-                                  array_elements=w["n_src"], array_pitch=w["pitch"])
-    t_build = time.perf_counter() - t0
-    K, C, M, gl, dt = m["K"], m["C"], m["M"], m["gl"], m["dt"]
-    n = K.shape[0]
+    models = [main] + subs
+    dt = min(m["dt"] for m in models)
     t = np.arange(n_t) * dt
     sig = model.toneburst(t, w["fc"], w["cycles"])
-    srcs = [model.global_indices(gl, nodes, 4) for nodes in m["src_nodes"]]
-    mons = model.global_indices(gl, m["mon_nodes"], 4)
-    R, q = len(srcs), mons.size
-    p_max = max(s.size for s in srcs)
+    R = w["n_src"]
     t0 = time.perf_counter()
-    plan32 = bfe_gb300.Plan(K, C, M, dt, bfe_gb300.VEL_CURRENT, "single", gl)
-    plan64 = bfe_gb300.Plan(K, C, M, dt, bfe_gb300.VEL_CURRENT, "double", gl)
+    plan32, offs = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], m["gl"]) for m in models], dt,
+                                        bfe_gb300.VEL_CURRENT, "single")
+    plan64, _ = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], None) for m in models], dt,
+                                     bfe_gb300.VEL_CURRENT, "double")
     t_plan = time.perf_counter() - t0
-
-    # device-resident inputs: one shared signal, forcing map, zeroed history
-    frc_dof = np.concatenate([s - 1 for s in srcs])
-    frc_rhs = np.concatenate([np.full(s.size, r) for r, s in enumerate(srcs)])
+    n = plan32.n
+    nnz = sum(m["K"].nnz for m in models)
+    # sources: RHS r drives element r of the array and source r of every sub-domain
+    srcs = []
+    for r in range(R):
+        parts = [model.global_indices(main["gl"], main["src_nodes"][r], 4)]
+        for k, m in enumerate(subs, start=1):
+            parts.append(model.global_indices(m["gl"], m["src_nodes"][r], 2) + offs[k])
+        srcs.append(np.concatenate(parts))
+    mon_parts = [model.global_indices(main["gl"], main["mon_nodes"], 4)]
+    for k, m in enumerate(subs, start=1):
+        mon_parts.append(model.global_indices(m["gl"], m["mon_nodes"], 2) + offs[k])
+    mons = np.concatenate(mon_parts)
+    mon_model = np.concatenate([np.full(p.size, k) for k, p in enumerate(mon_parts)])
+    q = mons.size
+    p_max = max(s_.size for s_ in srcs)
+    frc_dof = np.concatenate([s_ - 1 for s_ in srcs])
+    frc_rhs = np.concatenate([np.full(s_.size, r) for r, s_ in enumerate(srcs)])
     frc_sig = np.zeros(frc_dof.size, np.int64)
+    stream = torch.cuda.Stream()
     d_sig = torch.tensor(sig, dtype=torch.float64, device="cuda").reshape(n_t, 1)
     d_hist = torch.zeros((R, n_t, q), dtype=torch.float64, device="cuda")
-    nz = np.nonzero(sig)[0]
-    ti0 = int(nz.min())
+    ti0 = int(np.nonzero(sig)[0].min())
     steps_per_march = n_t - ti0
-    stream = torch.cuda.current_stream()
 
-    def march32():
-        d_hist.zero_()
-        plan32.run_device(R, n_t, ti0, frc_dof, frc_rhs, frc_sig, None, d_sig, mons - 1, d_hist,
-                          stream.cuda_stream)
+    def march32(plan=plan32, hist=d_hist, dofs=frc_dof, rhs=frc_rhs, fsig=frc_sig, mon=mons, r=R):
+        with torch.cuda.stream(stream):
+            hist.zero_()
+        plan.run_device(r, n_t, ti0, dofs, rhs, fsig, None, d_sig, mon - 1, hist, stream.cuda_stream)
 
     def barrier():
         if dist is not None:
@@ -253,18 +294,18 @@ def run_ours(args):
     step_avg_ms = stk["step_ms"] / max(stk["step_launches"], 1)
     aux_avg_ms = stk["aux_ms"] / max(stk["aux_launches"], 1)
     kname = KERNEL_NAMES.get(stk["variant"], "variant %d" % stk["variant"])
-    nnz = K.nnz
     bytes_step = algorithmic_bytes(nnz, n, R, p_max, q, 4)
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_step / (step_avg_ms * 1e-3) / 1e9
 
-    # plain FP64 form on the same model, one source (the middle element)
+    # plain FP64 form on the same models, one source (the middle element)
     r_mid = R // 2
     sel = frc_rhs == r_mid
     d_hist64 = torch.zeros((1, n_t, q), dtype=torch.float64, device="cuda")
 
     def march64():
-        d_hist64.zero_()
+        with torch.cuda.stream(stream):
+            d_hist64.zero_()
         plan64.run_device(1, n_t, ti0, frc_dof[sel], np.zeros(sel.sum(), np.int64),
                           frc_sig[sel], None, d_sig, mons - 1, d_hist64, stream.cuda_stream)
     march64()
@@ -287,31 +328,55 @@ def run_ours(args):
     aux64_ms = st64["aux_ms"] / max(st64["aux_launches"], 1)
     bytes64 = algorithmic_bytes(nnz, n, 1, srcs[r_mid].size, q, 8)
     h64 = d_hist64.cpu().numpy()[0]
-    err = float(np.abs(h32[r_mid] - h64).max() / np.abs(h64).max())
+    # max-normalised A-scan error per model (pressure and displacement differ in units)
+    errs = []
+    for k in range(len(models)):
+        c = mon_model == k
+        errs.append(float(np.abs(h32[r_mid][:, c] - h64[:, c]).max() / max(np.abs(h64[:, c]).max(), 1e-300)))
+    err = max(errs)
+
+    # the coupled FMC model alone (its own plan), same march
+    plan_a = bfe_gb300.Plan(main["K"], main["C"], main["M"], dt, bfe_gb300.VEL_CURRENT, "single", main["gl"])
+    selm = frc_dof < offs[1]
+    mons_a = mon_parts[0]
+    hist_a = torch.zeros((R, n_t, mons_a.size), dtype=torch.float64, device="cuda")
+    march32(plan_a, hist_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, R)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    march32(plan_a, hist_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, R)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_a = e0.elapsed_time(e1)
+    value_a = R * main["K"].shape[0] * steps_per_march / (ms_a * 1e-3)
+    plan_a.close()
 
     # end to end through the C ABI with host buffers (H2D signals, D2H A-scans)
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = 1
     th0 = time.perf_counter()
     for _ in range(e2e_steps):
-        hist_host = plan32.run_batched(t, [s for s in srcs], sig, mons)
+        plan32.run_batched(t, srcs, sig, mons)
     e2e_s = (time.perf_counter() - th0) / e2e_steps
     e2e_value = world * R * n * steps_per_march / e2e_s
-    h2d = 8 * n_t * R + 8 * (p_max * R + q)          # signals (repeated per source) + indices
+    h2d = 8 * n_t * R + 8 * (p_max * R + q)
     d2h = 8 * q * n_t * R
 
     result = None
     if rank == 0:
-        cpu = cpu_baseline(K, C, M, dt, t, srcs[r_mid], sig, mons) if world == 1 else None
+        cpu = cpu_baseline(main["K"], main["C"], main["M"], dt, t, srcs[r_mid][srcs[r_mid] <= offs[1]],
+                           sig, mons_a) if world == 1 else None
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "coupled water/steel 60x30 mm at 0.05 mm (1.44M triangles, "
-                                   "ASI2D2 interface, quadratic absorbers, void blob), 64-source "
-                                   "array FMC as 64 RHS, %d samples, FP32 batched" % n_t,
-                       "n_dof": n, "nnz_K": int(nnz), "sources": R, "monitors": q,
-                       "samples": n_t, "steps_marched_per_source": steps_per_march,
+            "config": {"workload": "batched multi-source and multi-model: coupled water/steel "
+                                   "60x30 mm at 0.05 mm (1.44M triangles, ASI2D2 interface, quadratic "
+                                   "absorbers, void blob) with a 64-element array, plus %d steel "
+                                   "scatterer sub-domain models of 50k-400k DOF (absorbers, void), "
+                                   "one plan, 64 sources as 64 RHS, %d samples, FP32 batched, CUDA graph"
+                                   % (len(subs), n_t),
+                       "n_dof": n, "nnz_K": int(nnz), "models": len(models), "sources": R,
+                       "monitors": q, "samples": n_t, "steps_marched_per_source": steps_per_march,
                        "l2": "inputs larger than L2 (state %.0f MB per time step)" % (3 * R * n * 4 / 1e6),
                        "parallelism": "replicas x%d" % world, "scale": args.scale},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -324,6 +389,8 @@ def run_ours(args):
                            "step_kernel_gbs": bytes64 / (step64_ms * 1e-3) / 1e9,
                            "speedup_fp32_batched": value / world / value64},
             "ascan_err_vs_fp64": err,
+            "coupled_fmc_only": {"value": value_a, "unit": UNIT, "ms_per_march": ms_a,
+                                 "n_dof": int(main["K"].shape[0])},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
             "gpu_launches": launches,

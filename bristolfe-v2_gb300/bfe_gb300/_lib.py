@@ -50,6 +50,10 @@ SIGNATURES = {
     "bfe_plan_create": (I32, [ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
                               ctypes.POINTER(BfeSparse), ctypes.c_double, I32, I32,
                               PI64, PI32, ctypes.POINTER(VP)]),
+    "bfe_plan_create_multi": (I32, [I32, ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
+                                    ctypes.POINTER(BfeSparse), ctypes.c_double, I32, I32,
+                                    ctypes.POINTER(PI64), ctypes.POINTER(PI32), PI64,
+                                    ctypes.POINTER(VP)]),
     "bfe_plan_destroy": (I32, [VP]),
     "bfe_plan_ndof": (I32, [VP, PI64]),
     "bfe_run": (I32, [VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, I32, PD, PD, PD]),

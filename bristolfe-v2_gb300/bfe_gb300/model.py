@@ -382,6 +382,52 @@ def coupled_water_steel(W=60e-3, H_water=20e-3, H_steel=10e-3, h=0.05e-3, fc=5e6
                 mon_dof=4, matls=matls, n_interface=ed.shape[0])
 
 
+def steel_subdomain(side, h=0.05e-3, fc=5e6, seed=0, n_src=64, n_mon=64, abs_wavelengths=3.0,
+                    blob_radius=1.5e-3, dof_to_use=(1, 2), damping_power_law=2):
+    """Square steel scatterer sub-domain model: absorbing layers on all four
+    sides (thickness min(3 wavelengths, side / 4), quadratic grading), a seeded
+    smooth void at the centre, n_src point sources (DOF 2) and n_mon monitors
+    (DOF 2) spread over the top surface inside the absorbers."""
+    rng = np.random.default_rng(seed)
+    nds, els = rect_mesh(0.0, side, 0.0, side, h)
+    D = isotropic_stiffness(STEEL["E"], STEEL["nu"])
+    matls = [dict(D=D, rho=STEEL["rho"])]
+    ctr = centroids(nds, els)
+    r = min(blob_radius, side / 8)
+    blob = smooth_blob(r, 8, 0.2, rng) + np.array([side / 2, side / 2])
+    keep = ~points_in_polygon(ctr, blob)
+    els = els[keep]
+    nds, els = remove_unused_nodes(nds, els)
+    ctr = centroids(nds, els)
+    cL = np.sqrt(D[0, 0] / STEEL["rho"])
+    thick = min(abs_wavelengths * cL / fc, side / 4)
+    inner = np.array([[thick, thick], [side - thick, thick], [side - thick, side - thick],
+                      [thick, side - thick]])
+    el_abs = np.clip(distance_to_polygon(ctr, inner) / thick, 0.0, 1.0)
+    el_abs[points_in_polygon(ctr, inner)] = 0.0
+    ne = els.shape[0]
+    typ = np.full(ne, TYPE_CODES["CPE3"])
+    K, C, M, gl = assemble(nds, els, np.ones(ne, np.int64), el_abs, typ, matls, dof_to_use,
+                           damping_power_law=damping_power_law)
+    dt = element_stable_dt(nds, els, D, STEEL["rho"])
+    top = np.nonzero(np.isclose(nds[:, 1], side))[0]
+    top = top[(nds[top, 0] >= thick) & (nds[top, 0] <= side - thick)]
+    top = top[np.argsort(nds[top, 0])]
+    src = top[np.linspace(0, top.size - 1, n_src).astype(int)] + 1
+    mon = top[np.linspace(0, top.size - 1, n_mon).astype(int)] + 1
+    return dict(nds=nds, els=els, K=K, C=C, M=M, gl=gl, dt=dt, src_nodes=[[s] for s in src],
+                src_dof=2, mon_nodes=mon, mon_dof=2)
+
+
+def subdomain_sides(n_models, dof_min=50e3, dof_max=400e3, h=0.05e-3, seed=1, dofs_per_node=2):
+    """Side lengths of square models whose DOF counts are log-uniform in
+    [dof_min, dof_max] (seeded)."""
+    rng = np.random.default_rng(seed)
+    dof = np.exp(rng.uniform(np.log(dof_min), np.log(dof_max), n_models))
+    nodes_per_side = np.sqrt(dof / dofs_per_node)
+    return (nodes_per_side - 1) * h
+
+
 def global_indices(gl, nodes, dof):
     """1-based global indices of (node, dof) pairs that exist (fn_BristolFE_v2.m:159-168)."""
     g = gl[np.asarray(nodes, np.int64) - 1, dof - 1]

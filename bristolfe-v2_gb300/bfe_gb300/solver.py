@@ -98,6 +98,48 @@ class Plan:
         check(lib.bfe_plan_ndof(self._h, ctypes.byref(nn)))
         self.n = nn.value
 
+    @classmethod
+    def multi(cls, models, dt, solver_mode=VEL_CURRENT, solver_precision="double"):
+        """One plan over independent models joined block-diagonally.
+
+        models: list of (K, C, M, gl_lookup or None). Returns (plan, offsets)
+        where model k's 1-based DOF i is plan DOF offsets[k] + i."""
+        lib = _lib.load()
+        self = cls.__new__(cls)
+        self._lib = lib
+        self.mode = _mode_code(solver_mode)
+        self.precision = _precision_code(solver_precision)
+        self.dt = float(dt)
+        nm = len(models)
+        Ks = (_lib.BfeSparse * nm)()
+        Cs = (_lib.BfeSparse * nm)()
+        Ms = (_lib.BfeSparse * nm)()
+        keep = []
+        nodes = (_lib.PI64 * nm)()
+        types = (_lib.PI32 * nm)()
+        have_nodes = all(mdl[3] is not None for mdl in models)
+        for k, (K, C, M, gl) in enumerate(models):
+            for arr, A in ((Ks, K), (Cs, C), (Ms, M)):
+                v, kp = _csr_view(A, "")
+                arr[k] = v
+                keep.append(kp)
+            if have_nodes:
+                nd, ty = dof_maps_from_lookup(gl, K.shape[0])
+                keep.append((nd, ty))
+                nodes[k] = ptr(nd, ctypes.c_int64)
+                types[k] = ptr(ty, ctypes.c_int32)
+        offs = np.zeros(nm + 1, np.int64)
+        handle = ctypes.c_void_p()
+        st = lib.bfe_plan_create_multi(nm, Ks, Cs, Ms, self.dt, self.mode, self.precision,
+                                       nodes if have_nodes else None, types if have_nodes else None,
+                                       ptr(offs, ctypes.c_int64), ctypes.byref(handle))
+        check(st)
+        self._h = handle
+        nn = ctypes.c_int64()
+        check(lib.bfe_plan_ndof(self._h, ctypes.byref(nn)))
+        self.n = nn.value
+        return self, offs
+
     def set_timing(self, enable=True):
         """CUDA-event timing of every launch in later runs (see stats())."""
         check(self._lib.bfe_plan_set_timing(self._h, int(bool(enable))))

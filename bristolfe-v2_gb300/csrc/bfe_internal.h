@@ -64,8 +64,15 @@ struct StepArgs {
   const void* u_n;
   const void* u_prev;
   void* u_new;
-  int64_t ti;                 // 0-based time index of the computed state
+  int64_t ti;                 // 0-based time index of the computed state, or (when
+                              // ti_dev is set) its offset from *ti_dev
+  const int64_t* ti_dev;      // device time-index base (graph replay) or nullptr
 };
+
+// Time index of the state a kernel computes.
+__device__ __forceinline__ int64_t step_index(const StepArgs& a) {
+  return a.ti_dev ? *a.ti_dev + a.ti : a.ti;
+}
 
 // Node-block operator (FP32 difference form): all DOF rows of one mesh node
 // are produced together from the neighbour DOF rows they couple to.
@@ -128,6 +135,7 @@ cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_
 cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t frame,
                          int field_is_vel, double dt, cudaStream_t s);
 cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
+cudaError_t launch_advance(int64_t* ti_dev, int64_t k, cudaStream_t s);
 
 // Message returned by bfe_last_error() on the calling thread.
 void set_last_error(const char* msg);

@@ -43,7 +43,7 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t* a, int n, int key)
 template <typename T>
 __device__ __forceinline__ T forcing_sum(const StepArgs& a, int i, int r) {
   const T* coef = static_cast<const T*>(a.frc_coef);
-  const T* sig = static_cast<const T*>(a.sig) + (size_t)a.ti * a.n_sig;
+  const T* sig = static_cast<const T*>(a.sig) + (size_t)step_index(a) * a.n_sig;
   T f = T(0);
   for (int e = lower_bound_i32(a.frc_row, a.n_frc, i); e < a.n_frc && __ldg(a.frc_row + e) == i; ++e) {
     if (__ldg(a.frc_rhs + e) == r) f += __ldg(coef + e) * __ldg(sig + __ldg(a.frc_sig + e));
@@ -54,7 +54,7 @@ __device__ __forceinline__ T forcing_sum(const StepArgs& a, int i, int r) {
 __device__ __forceinline__ void write_history(const StepArgs& a, int i, int r, double v) {
   for (int k = lower_bound_i32(a.mon_row, a.n_mon, i); k < a.n_mon && __ldg(a.mon_row + k) == i; ++k) {
     int slot = __ldg(a.mon_slot + k);
-    a.hist[(size_t)slot + (size_t)a.q * ((size_t)a.ti + (size_t)a.n_t * r)] = v;
+    a.hist[(size_t)slot + (size_t)a.q * ((size_t)step_index(a) + (size_t)a.n_t * r)] = v;
   }
 }
 
@@ -873,6 +873,30 @@ __global__ void __launch_bounds__(256) interface_fixup(StepArgs a) {
   if (__ldg(a.rowinfo + row) & kRowMonitored) write_history(a, row, c, (double)r);
 }
 
+// Interface correction for one right-hand side: one warp per interface row,
+// lanes stride over the row of Z and reduce with shuffles.
+template <typename T>
+__global__ void __launch_bounds__(256) interface_fixup_r1(StepArgs a) {
+  const int t = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= a.n_int) return;
+  const int row = __ldg(a.int_row + t);
+  const T* z = static_cast<const T*>(a.z_val);
+  const T* v = static_cast<const T*>(a.v_int);
+  T acc = T(0);
+  for (int e = __ldg(a.z_ptr + t) + lane; e < __ldg(a.z_ptr + t + 1); e += 32)
+    acc += __ldg(z + e) * v[__ldg(a.z_col + e)];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if (lane == 0) {
+    T* unew = static_cast<T*>(a.u_new);
+    const T base = a.int_base_prev ? static_cast<const T*>(a.u_prev)[row] : unew[row];
+    const T r = base + acc;
+    unew[row] = r;
+    if (__ldg(a.rowinfo + row) & kRowMonitored) write_history(a, row, 0, (double)r);
+  }
+}
+
 // Field frame: fld[i + n * frame] = (u_new - u_n) / dt or u_new (R = 1).
 template <typename T>
 __global__ void frame_kernel(StepArgs a, double* fld, int64_t frame, int is_vel, double dt) {
@@ -882,6 +906,8 @@ __global__ void frame_kernel(StepArgs a, double* fld, int64_t frame, int is_vel,
   const double uo = (double)static_cast<const T*>(a.u_n)[i];
   fld[(size_t)i + (size_t)a.n * frame] = is_vel ? (un - uo) / dt : un;
 }
+
+__global__ void advance_kernel(int64_t* ti_dev, int64_t k) { *ti_dev += k; }
 
 __global__ void cast_kernel(const double* in, float* out, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -992,6 +1018,12 @@ cudaError_t set_batched_smem_limit(int precision, size_t smem) {
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t st) {
   if (a.n_int == 0) return cudaSuccess;
   const int threads = 256;
+  if (a.R == 1) {
+    const int blocks = (int)(((int64_t)a.n_int * 32 + threads - 1) / threads);
+    if (precision == 0) interface_fixup_r1<double><<<blocks, threads, 0, st>>>(a);
+    else interface_fixup_r1<float><<<blocks, threads, 0, st>>>(a);
+    return cudaGetLastError();
+  }
   const int64_t total = (int64_t)a.n_int * a.R;
   const int blocks = (int)((total + threads - 1) / threads);
   if (precision == 0) interface_fixup<double><<<blocks, threads, 0, st>>>(a);
@@ -1005,6 +1037,11 @@ cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t 
   const int blocks = (a.n + threads - 1) / threads;
   if (precision == 0) frame_kernel<double><<<blocks, threads, 0, st>>>(a, fld, frame, field_is_vel, dt);
   else frame_kernel<float><<<blocks, threads, 0, st>>>(a, fld, frame, field_is_vel, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_advance(int64_t* ti_dev, int64_t k, cudaStream_t st) {
+  advance_kernel<<<1, 1, 0, st>>>(ti_dev, k);
   return cudaGetLastError();
 }
 

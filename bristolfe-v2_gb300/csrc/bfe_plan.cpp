@@ -775,6 +775,70 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   return BFE_OK;
 }
 
+int bfe_plan_create_multi(int32_t n_models, const bfe_sparse* K, const bfe_sparse* C,
+                          const bfe_sparse* M, double dt, int32_t solver_mode, int32_t precision,
+                          const int64_t* const* dof_node, const int32_t* const* dof_type,
+                          int64_t* row_offsets, bfe_plan** out) {
+  g_last_error.clear();
+  if (n_models < 1 || !K || !C || !M || !row_offsets || !out)
+    return fail(BFE_ERR_ARG, "invalid arguments to bfe_plan_create_multi");
+  // join the models block-diagonally as CSR (each input converted first)
+  std::vector<Csr> ks(n_models), cs(n_models), ms(n_models);
+  int rc;
+  int64_t n = 0;
+  row_offsets[0] = 0;
+  for (int32_t k = 0; k < n_models; ++k) {
+    if ((rc = to_csr(&K[k], "K", ks[k])) || (rc = to_csr(&C[k], "C", cs[k])) || (rc = to_csr(&M[k], "M", ms[k])))
+      return fail(rc, "model %d: %s", k, g_last_error.c_str());
+    if (ks[k].n != ks[k].m || cs[k].n != ks[k].n || ms[k].n != ks[k].n || cs[k].m != ks[k].n || ms[k].m != ks[k].n)
+      return fail(BFE_ERR_ARG, "model %d: K, C and M must be square and of equal size", k);
+    n += ks[k].n;
+    row_offsets[k + 1] = n;
+  }
+  auto join = [&](std::vector<Csr>& parts, std::vector<int64_t>& p, std::vector<int64_t>& ix, std::vector<double>& v) {
+    p.assign(1, 0);
+    for (int32_t k = 0; k < n_models; ++k) {
+      const int64_t off = row_offsets[k];
+      for (int64_t i = 0; i < parts[k].n; ++i) {
+        for (int64_t e = parts[k].ptr[i]; e < parts[k].ptr[i + 1]; ++e) {
+          ix.push_back(parts[k].idx[e] + off);
+          v.push_back(parts[k].val[e]);
+        }
+        p.push_back((int64_t)ix.size());
+      }
+      parts[k] = Csr();
+    }
+  };
+  std::vector<int64_t> kp, ki, cp, ci, mp, mi;
+  std::vector<double> kv, cv, mv;
+  join(ks, kp, ki, kv);
+  join(cs, cp, ci, cv);
+  join(ms, mp, mi, mv);
+  const bfe_sparse Kj{n, n, (int64_t)kv.size(), BFE_CSR, kp.data(), ki.data(), kv.data()};
+  const bfe_sparse Cj{n, n, (int64_t)cv.size(), BFE_CSR, cp.data(), ci.data(), cv.data()};
+  const bfe_sparse Mj{n, n, (int64_t)mv.size(), BFE_CSR, mp.data(), mi.data(), mv.data()};
+  std::vector<int64_t> node;
+  std::vector<int32_t> type;
+  bool have = dof_node && dof_type;
+  if (have) {
+    node.resize(n);
+    type.resize(n);
+    int64_t node_base = 0;
+    for (int32_t k = 0; k < n_models && have; ++k) {
+      if (!dof_node[k] || !dof_type[k]) { have = false; break; }
+      int64_t mx = -1;
+      for (int64_t i = 0; i < row_offsets[k + 1] - row_offsets[k]; ++i) {
+        node[row_offsets[k] + i] = dof_node[k][i] + node_base;
+        type[row_offsets[k] + i] = dof_type[k][i];
+        mx = std::max(mx, dof_node[k][i]);
+      }
+      node_base += mx + 1;
+    }
+  }
+  return bfe_plan_create(&Kj, &Cj, &Mj, dt, solver_mode, precision, have ? node.data() : nullptr,
+                         have ? type.data() : nullptr, out);
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1012,29 +1076,29 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     }
   }
   stt.variant = variant;
-  for (int64_t ti = rs.ti_start; ti < rs.n_t; ++ti) {
-    a.ti = ti;
+  // One time step: step kernel, interface correction, optional frame.
+  auto one_step = [&](int64_t ti, bool rec) -> int {
     a.u_prev = U[iprev];
     a.u_n = U[icur];
     a.u_new = U[inew];
-    if (timing) CUDA_TRY(mark(ev_step));
+    if (rec && timing) CUDA_TRY(mark(ev_step));
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st) : launch_batched(gp, grp, variant, icur, iprev);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
-    if (timing) CUDA_TRY(mark(ev_step));
+    if (rec && timing) CUDA_TRY(mark(ev_step));
     stt.step_launches++;
     if (pl->n_int) {
-      if (timing) CUDA_TRY(mark(ev_aux));
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
       e = bfe::launch_interface_fixup(a, prec, st);
       if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "interface kernel launch failed: %s", cudaGetErrorString(e));
-      if (timing) CUDA_TRY(mark(ev_aux));
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
       stt.aux_launches++;
     }
-    if (rs.every_n > 0 && rs.d_fld && ti % rs.every_n == 0) {
+    if (ti >= 0 && rs.every_n > 0 && rs.d_fld && ti % rs.every_n == 0) {
       const int64_t k = ti / rs.every_n;
-      if (timing) CUDA_TRY(mark(ev_aux));
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
       e = bfe::launch_frame(a, prec, rs.d_fld, k, rs.field_is_vel, pl->dt, st);
       if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "frame kernel launch failed: %s", cudaGetErrorString(e));
-      if (timing) CUDA_TRY(mark(ev_aux));
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
       stt.aux_launches++;
       if (rs.fld_time) (*rs.fld_time)[k] = rs.time[ti];
     }
@@ -1042,6 +1106,58 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     iprev = icur;
     icur = inew;
     inew = t;
+    return BFE_OK;
+  };
+  int64_t ti = rs.ti_start;
+  // CUDA graph replay: the launches of kGraphSteps consecutive steps (a
+  // multiple of the 3-buffer rotation) are captured once, with the time index
+  // read from a device counter that the last node advances, and replayed.
+  // Not used with per-launch timing, field frames or the legacy stream.
+  const int64_t kGraphSteps = 48;
+  const bool use_graph = !timing && rs.every_n <= 0 && st != nullptr && st != cudaStreamLegacy &&
+                         (rs.n_t - rs.ti_start) >= 2 * kGraphSteps && getenv("BFE_NO_GRAPH") == nullptr;
+  DevBuf<int64_t> d_ti;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphGuard {
+    cudaGraph_t* g; cudaGraphExec_t* x;
+    ~GraphGuard() { if (*x) cudaGraphExecDestroy(*x); if (*g) cudaGraphDestroy(*g); }
+  } gguard{&graph, &gexec};
+  if (use_graph) {
+    CUDA_TRY(d_ti.alloc(1));
+    const int64_t t0 = rs.ti_start;
+    CUDA_TRY(cudaMemcpyAsync(d_ti.p, &t0, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    a.ti_dev = d_ti.p;
+    const int64_t launches0 = stt.step_launches, aux0 = stt.aux_launches;
+    int rc2 = BFE_OK;
+    for (int64_t k = 0; k < kGraphSteps && rc2 == BFE_OK; ++k) {
+      a.ti = k;
+      rc2 = one_step(-1, false);
+    }
+    if (rc2 == BFE_OK && bfe::launch_advance(d_ti.p, kGraphSteps, st) != cudaSuccess)
+      rc2 = fail(BFE_ERR_CUDA, "graph capture failed");
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    graph = g;
+    if (rc2) return rc2;
+    CUDA_TRY(ce);
+    CUDA_TRY(cudaGraphInstantiate(&gexec, graph, 0));
+    const int64_t per_step = stt.step_launches - launches0, per_aux = stt.aux_launches - aux0;
+    stt.step_launches = launches0;
+    stt.aux_launches = aux0;
+    const int64_t reps = (rs.n_t - rs.ti_start) / kGraphSteps;
+    for (int64_t r = 0; r < reps; ++r) CUDA_TRY(cudaGraphLaunch(gexec, st));
+    stt.step_launches += reps * per_step;
+    stt.aux_launches += reps * (per_aux + 1);
+    ti = rs.ti_start + reps * kGraphSteps;      // rotation is back where it started
+    a.ti_dev = nullptr;
+  }
+  for (; ti < rs.n_t; ++ti) {
+    a.ti = ti;
+    const int rc3 = one_step(ti, true);
+    if (rc3) return rc3;
   }
   CUDA_TRY(cudaStreamSynchronize(st));
   if (have_tmaps) {

@@ -98,7 +98,7 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t* a, int n, int key)
 
 __device__ __forceinline__ float forcing_f32(const StepArgs& a, int i, int r) {
   const float* coef = static_cast<const float*>(a.frc_coef);
-  const float* sig = static_cast<const float*>(a.sig) + (size_t)a.ti * a.n_sig;
+  const float* sig = static_cast<const float*>(a.sig) + (size_t)step_index(a) * a.n_sig;
   float f = 0.f;
   for (int e = lower_bound_i32(a.frc_row, a.n_frc, i); e < a.n_frc && __ldg(a.frc_row + e) == i; ++e)
     if (__ldg(a.frc_rhs + e) == r) f += __ldg(coef + e) * __ldg(sig + __ldg(a.frc_sig + e));
@@ -107,7 +107,7 @@ __device__ __forceinline__ float forcing_f32(const StepArgs& a, int i, int r) {
 
 __device__ __forceinline__ void history(const StepArgs& a, int i, int r, double v) {
   for (int k = lower_bound_i32(a.mon_row, a.n_mon, i); k < a.n_mon && __ldg(a.mon_row + k) == i; ++k)
-    a.hist[(size_t)__ldg(a.mon_slot + k) + (size_t)a.q * ((size_t)a.ti + (size_t)a.n_t * r)] = v;
+    a.hist[(size_t)__ldg(a.mon_slot + k) + (size_t)a.q * ((size_t)step_index(a) + (size_t)a.n_t * r)] = v;
 }
 
 struct TItem {

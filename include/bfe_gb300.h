@@ -85,6 +85,20 @@ int bfe_plan_create(const bfe_sparse* K, const bfe_sparse* C, const bfe_sparse* 
                     const int64_t* dof_node, const int32_t* dof_type,
                     bfe_plan** out);
 
+/*
+ * One plan over several independent models (sub-domain and scatterer models,
+ * subdoms/fn_run_subdomain_model.m:26-116, which the reference runs one after
+ * the other): the operators are joined block-diagonally, so every step kernel
+ * marches all models at once. Model k's DOF i is row row_offsets[k] + i of
+ * the plan (row_offsets has n_models + 1 entries, filled on return). All
+ * models share dt. dof_node / dof_type may be NULL, or arrays of n_models
+ * pointers (each may be NULL) as in bfe_plan_create.
+ */
+int bfe_plan_create_multi(int32_t n_models, const bfe_sparse* K, const bfe_sparse* C,
+                          const bfe_sparse* M, double dt, int32_t solver_mode, int32_t precision,
+                          const int64_t* const* dof_node, const int32_t* const* dof_type,
+                          int64_t* row_offsets, bfe_plan** out);
+
 int bfe_plan_destroy(bfe_plan* plan);
 
 /* Number of global DOFs of a plan. */

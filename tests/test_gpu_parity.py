@@ -194,3 +194,43 @@ def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
         h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
         assert _err(hb[:q4, :, r], h0[:q4]) <= TOL32
         assert _err(hb[q4:, :, r], h0[q4:]) <= TOL32
+
+
+@pytest.mark.parametrize("prec,tol", [("double", TOL64), ("single", TOL32)])
+def test_multi_model_plan_matches_each_model(bfe, plate, coupled, prec, tol):
+    """Independent models joined block-diagonally in one plan: each model's
+    A-scans equal its own oracle run."""
+    nt = 240
+    t, s = modelgen.pulse(nt, min(plate["dt"], coupled["dt"]))
+    dt = t[1] - t[0]
+    plan, offs = bfe.Plan.multi([(plate["K"], plate["C"], plate["M"], plate["gl"]),
+                                 (coupled["K"], coupled["C"], coupled["M"], coupled["gl"])],
+                                dt, osolver.VEL_CURRENT, prec)
+    with plan:
+        f0 = modelgen.gi_of(plate["gl"], [plate["frc_nd"]], 2)
+        f1 = modelgen.gi_of(coupled["gl"], [coupled["frc_nd"]], 4)
+        h0i = modelgen.gi_of(plate["gl"], plate["mon_nds"], 2)
+        h1i = modelgen.gi_of(coupled["gl"], coupled["mon_nds"], 4)
+        hist = plan.run_batched(t, [f0, f1 + offs[1]], s, np.concatenate([h0i, h1i + offs[1]]))
+    for k, (m, fi, hi) in enumerate(((plate, f0, h0i), (coupled, f1, h1i))):
+        mm = dict(m)
+        ref, _, _, _ = osolver.explicit_dynamic_solver_v6(m["K"], m["C"], m["M"], t, fi, s, [], [], hi,
+                                                          np.inf, 0, "KE", osolver.VEL_CURRENT)
+        got = hist[:h0i.size, :, 0] if k == 0 else hist[h0i.size:, :, 1]
+        assert _err(got, ref) <= tol
+    # the other model's source does not leak across the block diagonal
+    assert np.all(hist[:h0i.size, :, 1] == 0) and np.all(hist[h0i.size:, :, 0] == 0)
+
+
+@pytest.mark.parametrize("prec", ["double", "single"])
+def test_graph_replay_equals_plain_launches(bfe, coupled, prec, monkeypatch):
+    m = coupled
+    nt = 400                                   # >= 2 graph chunks of 48 steps plus a tail
+    t, s = modelgen.pulse(nt, m["dt"])
+    srcs = [modelgen.gi_of(m["gl"], [nd], 4) for nd in m["mon_nds"][:3]]
+    hi = modelgen.gi_of(m["gl"], m["mon_nds"], 4)
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, prec, m["gl"]) as plan:
+        hg = plan.run_batched(t, srcs, s, hi)
+        monkeypatch.setenv("BFE_NO_GRAPH", "1")
+        hp = plan.run_batched(t, srcs, s, hi)
+    assert np.array_equal(hg, hp)
