@@ -133,9 +133,12 @@ def test_batched_sources_equal_single_runs(bfe, coupled, prec):
                          modelgen.gi_of(m["gl"], m["mon_nds"], 2)])
     with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, prec, m["gl"]) as plan:
         hb = plan.run_batched(t, srcs, s, hi)
+        # the one-source path sums the interface correction in another order,
+        # so the paths agree to the rounding of the precision
+        same = 1e-12 if prec == "double" else 1e-6
         for r, fi in enumerate(srcs):
             h1, _, _ = plan.run(t, fi, s, hi)
-            assert np.abs(hb[:, :, r] - h1).max() <= 1e-12 * max(np.abs(h1).max(), 1e-300)
+            assert np.abs(hb[:, :, r] - h1).max() <= same * max(np.abs(h1).max(), 1e-300)
     # and against the oracle for one source
     h0, _, _, _ = _oracle(m, t, srcs[1], s, hi)
     q4 = modelgen.gi_of(m["gl"], m["mon_nds"], 4).size
