@@ -387,7 +387,7 @@ def steel_subdomain(side, h=0.05e-3, fc=5e6, seed=0, n_src=64, n_mon=64, abs_wav
     """Square steel scatterer sub-domain model: absorbing layers on all four
     sides (thickness min(3 wavelengths, side / 4), quadratic grading), a seeded
     smooth void at the centre, n_src point sources (DOF 2) and n_mon monitors
-    (DOF 2) spread over the top surface inside the absorbers."""
+    (DOF 2) spread along a line just inside the absorbing frame, near its top."""
     rng = np.random.default_rng(seed)
     nds, els = rect_mesh(0.0, side, 0.0, side, h)
     D = isotropic_stiffness(STEEL["E"], STEEL["nu"])
@@ -410,11 +410,15 @@ def steel_subdomain(side, h=0.05e-3, fc=5e6, seed=0, n_src=64, n_mon=64, abs_wav
     K, C, M, gl = assemble(nds, els, np.ones(ne, np.int64), el_abs, typ, matls, dof_to_use,
                            damping_power_law=damping_power_law)
     dt = element_stable_dt(nds, els, D, STEEL["rho"])
-    top = np.nonzero(np.isclose(nds[:, 1], side))[0]
-    top = top[(nds[top, 0] >= thick) & (nds[top, 0] <= side - thick)]
-    top = top[np.argsort(nds[top, 0])]
-    src = top[np.linspace(0, top.size - 1, n_src).astype(int)] + 1
-    mon = top[np.linspace(0, top.size - 1, n_mon).astype(int)] + 1
+    # transducer line just inside the absorbing frame (the driven boundary of
+    # a sub-domain lies inside its absorbers, subdoms/fn_create_subdomain.m)
+    y_line = side - thick - 2 * h
+    row = np.abs(nds[:, 1] - y_line)
+    line = np.nonzero(row <= row.min() + 1e-12)[0]
+    line = line[(nds[line, 0] >= thick + 2 * h) & (nds[line, 0] <= side - thick - 2 * h)]
+    line = line[np.argsort(nds[line, 0])]
+    src = line[np.linspace(0, line.size - 1, n_src).astype(int)] + 1
+    mon = line[np.linspace(0, line.size - 1, n_mon).astype(int)] + 1
     return dict(nds=nds, els=els, K=K, C=C, M=M, gl=gl, dt=dt, src_nodes=[[s] for s in src],
                 src_dof=2, mon_nodes=mon, mon_dof=2)
 
