@@ -436,3 +436,141 @@ def global_indices(gl, nodes, dof):
     """1-based global indices of (node, dof) pairs that exist (fn_BristolFE_v2.m:159-168)."""
     g = gl[np.asarray(nodes, np.int64) - 1, dof - 1]
     return g[g > 0]
+
+
+# ---------------------------------------------------------------------------
+# 3D structured solid (8-node bricks)
+
+_BRICK = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                   [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], np.int64)
+
+
+def brick_matrices(dx, dy, dz, D, rho):
+    """Stiffness (24 x 24, node-major, DOF-minor) and lumped nodal mass of one
+    trilinear brick of sides dx, dy, dz: 2 x 2 x 2 Gauss integration of
+    B' D B with the Voigt order [11, 22, 33, 23, 13, 12] (engineering shear);
+    lumped mass = rho * V / 8 per node."""
+    g = 1.0 / np.sqrt(3.0)
+    sgn = 2 * _BRICK - 1                           # natural coordinates of the nodes
+    h = np.array([dx, dy, dz], float)
+    K = np.zeros((24, 24))
+    detJ = dx * dy * dz / 8.0
+    for q in np.array(np.meshgrid([-g, g], [-g, g], [-g, g], indexing="ij")).reshape(3, -1).T:
+        # dN/dx_d = sgn_d * prod_{e != d}(1 + sgn_e q_e) / 8 * (2 / h_d)
+        f = 1 + sgn * q
+        dN = np.stack([sgn[:, d] * np.prod(np.delete(f, d, axis=1), axis=1) / 8 * (2 / h[d])
+                       for d in range(3)], axis=1)                    # (8, 3)
+        B = np.zeros((6, 24))
+        for a in range(8):
+            c = 3 * a
+            B[0, c], B[1, c + 1], B[2, c + 2] = dN[a]
+            B[3, c + 1], B[3, c + 2] = dN[a, 2], dN[a, 1]
+            B[4, c], B[4, c + 2] = dN[a, 2], dN[a, 0]
+            B[5, c], B[5, c + 1] = dN[a, 1], dN[a, 0]
+        K += B.T @ D @ B * detJ
+    return K, rho * dx * dy * dz / 8.0
+
+
+def cubic_mesh(x1, y1, z1, h):
+    """Node and brick layout of a structured box [0, x1] x [0, y1] x [0, z1]
+    with the reference's ordering (fn_3d_cubic_structured_mesh.m: node
+    index i + nx (j + ny k), 1-based, bricks i fastest)."""
+    sz = np.array([x1, y1, z1], float)
+    n = (np.ceil(sz / h) + 1).astype(np.int64)
+    d = sz / (n - 1)
+    i, j, k = np.meshgrid(np.arange(n[0]), np.arange(n[1]), np.arange(n[2]), indexing="ij")
+    nds = np.column_stack([i.ravel(order="F") * d[0], j.ravel(order="F") * d[1], k.ravel(order="F") * d[2]])
+    ei, ej, ek = np.meshgrid(np.arange(n[0] - 1), np.arange(n[1] - 1), np.arange(n[2] - 1), indexing="ij")
+    ei, ej, ek = (x.ravel(order="F") for x in (ei, ej, ek))
+    els = np.column_stack([(ei + o[0]) + n[0] * ((ej + o[1]) + n[1] * (ek + o[2])) + 1 for o in _BRICK])
+    return nds, els, n, d
+
+
+def assemble_brick_grid(n, d, D, rho, el_abs, damping_power_law=3, max_damping=3.1415e7,
+                        max_stiffness_reduction=0.01):
+    """Global K, C, M (CSR, DOF = 3 node + dof) of a structured brick grid with
+    per-element absorbing index el_abs (grid order). Every brick shares one
+    element matrix; the absorbing grading scales it per element
+    (fn_build_global_matrices_v5.m:115-116), so K is accumulated as 27-point
+    node-block stencils with array slices instead of a COO sort."""
+    nx, ny, nz = (int(v) for v in n)
+    ke, me = brick_matrices(d[0], d[1], d[2], D, rho)
+    a = np.asarray(el_abs, float).reshape(nx - 1, ny - 1, nz - 1, order="F")
+    s = np.exp(np.log(max_stiffness_reduction) * a ** (damping_power_law + 1))
+    cfac = a ** damping_power_law * max_damping
+    Kb = np.zeros((nx, ny, nz, 27, 3, 3))
+    mn = np.zeros((nx, ny, nz))
+    cn = np.zeros((nx, ny, nz))
+    for ia, oa in enumerate(_BRICK):
+        sa = (slice(oa[0], oa[0] + nx - 1), slice(oa[1], oa[1] + ny - 1), slice(oa[2], oa[2] + nz - 1))
+        mn[sa] += me
+        cn[sa] += me * cfac
+        for ib, ob in enumerate(_BRICK):
+            off = ob - oa
+            slot = (off[0] + 1) + 3 * (off[1] + 1) + 9 * (off[2] + 1)
+            Kb[sa + (slot,)] += s[..., None, None] * ke[3 * ia:3 * ia + 3, 3 * ib:3 * ib + 3]
+    # CSR rows: node-major, dof-minor; columns sorted (neighbour node index, dof)
+    nn = nx * ny * nz
+    node = np.arange(nn)
+    ci, cj, ck = node % nx, (node // nx) % ny, node // (nx * ny)
+    Kf = Kb.reshape(nx * ny * nz, 27, 3, 3, order="F")
+    rows, cols, vals = [], [], []
+    for slot in range(27):
+        o = np.array([slot % 3 - 1, (slot // 3) % 3 - 1, slot // 9 - 1])
+        ok = (ci + o[0] >= 0) & (ci + o[0] < nx) & (cj + o[1] >= 0) & (cj + o[1] < ny) & \
+             (ck + o[2] >= 0) & (ck + o[2] < nz)
+        src = node[ok]
+        nb = src + o[0] + nx * (o[1] + ny * o[2])
+        blk = Kf[src, slot]                                       # (m, 3, 3)
+        for r in range(3):
+            for c in range(3):
+                rows.append(3 * src + r)
+                cols.append(3 * nb + c)
+                vals.append(blk[:, r, c])
+    N = 3 * nn
+    K = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
+    K.sum_duplicates()
+    K.eliminate_zeros()
+    mvec = np.repeat(mn.ravel(order="F"), 3)
+    cvec = np.repeat(cn.ravel(order="F"), 3)
+    M = sp.diags(mvec).tocsr()
+    C = sp.diags(cvec).tocsr()
+    C.eliminate_zeros()
+    gl = (3 * node[:, None] + np.arange(3)[None, :] + 1).astype(np.int64)
+    return K, C, M, gl
+
+
+def box_distance(pts, lo, hi):
+    """Euclidean distance from points to an axis-aligned box (0 inside)."""
+    dlo = np.maximum(lo - pts, 0.0)
+    dhi = np.maximum(pts - hi, 0.0)
+    return np.sqrt(((dlo + dhi) ** 2).sum(1))
+
+
+def steel_block_3d(Lx=10e-3, Ly=10e-3, Lz=5e-3, h=0.1e-3, fc=5e6, abs_wavelengths=3.0,
+                   n_mon=64, damping_power_law=3):
+    """3D steel block of 8-node bricks: absorbing layers on the four sides and
+    the bottom (thickness in longitudinal wavelengths, capped at a quarter of
+    the smaller side), a point force normal to the top face (DOF 3) at its
+    centre, n_mon monitors on a square grid of top-face nodes."""
+    nds, els, n, d = cubic_mesh(Lx, Ly, Lz, h)
+    D = isotropic_stiffness(STEEL["E"], STEEL["nu"])
+    cL = np.sqrt(D[0, 0] / STEEL["rho"])
+    thick = min(abs_wavelengths * cL / fc, min(Lx, Ly) / 4, Lz / 2)
+    ctr = centroids(nds, els)
+    lo = np.array([thick, thick, thick])
+    hi = np.array([Lx - thick, Ly - thick, np.inf])
+    el_abs = np.clip(box_distance(ctr, lo, hi) / thick, 0.0, 1.0)
+    K, C, M, gl = assemble_brick_grid(n, d, D, STEEL["rho"], el_abs, damping_power_law)
+    ke, me = brick_matrices(d[0], d[1], d[2], D, STEEL["rho"])
+    lam = np.linalg.eigvalsh(ke / me).max()
+    dt = 0.9 * 2.0 / np.sqrt(lam)
+    top = np.nonzero(np.isclose(nds[:, 2], Lz))[0]
+    src = top[np.argmin((nds[top, 0] - Lx / 2) ** 2 + (nds[top, 1] - Ly / 2) ** 2)]
+    side = int(round(np.sqrt(n_mon)))
+    gx = np.linspace(thick, Lx - thick, side)
+    gy = np.linspace(thick, Ly - thick, side)
+    mon = np.array([top[np.argmin((nds[top, 0] - x) ** 2 + (nds[top, 1] - y) ** 2)]
+                    for y in gy for x in gx]) + 1
+    return dict(nds=nds, els=els, el_abs=el_abs, K=K, C=C, M=M, gl=gl, dt=dt,
+                src_nodes=[src + 1], src_dof=3, mon_nodes=mon, mon_dof=3)

@@ -88,12 +88,23 @@ int to_csr(const bfe_sparse* A, const char* name, Csr& out) {
     ci[p] = cols[e];
     cv[p] = A->val[e];
   }
-  // sort each row, sum duplicates, drop exact zeros (MATLAB keeps non-zeros)
+  // sort each row, sum duplicates, drop exact zeros (MATLAB keeps non-zeros);
+  // rows that are already strictly increasing are copied as they are
   std::vector<int64_t> nptr(out.n + 1, 0);
   out.idx.clear();
   out.val.clear();
+  out.idx.reserve(ci.size());
+  out.val.reserve(ci.size());
   std::vector<std::pair<int64_t, double>> tmp;
   for (int64_t i = 0; i < out.n; ++i) {
+    bool sorted = true;
+    for (int64_t e = out.ptr[i] + 1; e < out.ptr[i + 1] && sorted; ++e) sorted = ci[e] > ci[e - 1];
+    if (sorted) {
+      for (int64_t e = out.ptr[i]; e < out.ptr[i + 1]; ++e)
+        if (cv[e] != 0.0) { out.idx.push_back(ci[e]); out.val.push_back(cv[e]); }
+      nptr[i + 1] = (int64_t)out.idx.size();
+      continue;
+    }
     tmp.clear();
     for (int64_t e = out.ptr[i]; e < out.ptr[i + 1]; ++e) tmp.emplace_back(ci[e], cv[e]);
     std::sort(tmp.begin(), tmp.end(), [](auto& x, auto& y) { return x.first < y.first; });
@@ -510,17 +521,26 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         // node block and every per-type partial row sum of K vanishes
         bool diff = have_nodes;
         if (diff) {
-          std::map<int32_t, std::pair<double, double>> sums;  // type -> (sum, abs sum)
-          for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
-            auto& sm = sums[dof_type[K.idx[e]]];
-            sm.first += K.val[e];
-            sm.second += std::fabs(K.val[e]);
+          // per DOF type of the columns: (type, sum, abs sum); few types per row
+          int32_t ty[16];
+          double sm[16], sa[16];
+          int nty = 0;
+          for (int64_t e = K.ptr[i]; e < K.ptr[i + 1] && diff; ++e) {
+            const int32_t t = dof_type[K.idx[e]];
+            int k = 0;
+            while (k < nty && ty[k] != t) ++k;
+            if (k == nty) {
+              if (nty == 16) { diff = false; break; }
+              ty[nty] = t; sm[nty] = 0.0; sa[nty] = 0.0; ++nty;
+            }
+            sm[k] += K.val[e];
+            sa[k] += std::fabs(K.val[e]);
           }
-          for (auto& kv : sums) {
+          for (int k = 0; k < nty && diff; ++k) {
             bool found = false;
-            for (int64_t k = blk_base[i]; k < blk_base[i] + blk_len[i]; ++k)
-              if (dof_type[k] == kv.first) found = true;
-            if (!found || std::fabs(kv.second.first) > 1e-9 * kv.second.second) diff = false;
+            for (int64_t b = blk_base[i]; b < blk_base[i] + blk_len[i]; ++b)
+              if (dof_type[b] == ty[k]) found = true;
+            if (!found || std::fabs(sm[k]) > 1e-9 * sa[k]) diff = false;
           }
         }
         if (diff) {
