@@ -60,6 +60,8 @@ SIGNATURES = {
     "bfe_run_batched": (I32, [VP, I64, I64, PD, I64, PI64, I64, PD, I64, PI64, PD]),
     "bfe_run_device": (I32, [VP, I64, I64, I64, I64, PI64, PI64, PI64, PD, I64, VP,
                              I64, PI64, VP, VP]),
+    "bfe_adjoint_gradient": (I32, [VP, I64, I32, PI64, PD, PD, PD, I64, I64, PD, I64, PI64, I64, PD,
+                                   I64, PI64, PD, I64, PD, PD, PD, PD]),
     "bfe_run_f64_noalloc": (I32, [I64, VP, VP, VP, VP, I64, I64, I64, VP, VP, VP, I64, VP, VP, VP]),
     "bfe_plan_set_timing": (I32, [VP, I32]),
     "bfe_plan_stats": (I32, [VP, ctypes.POINTER(BfeStats)]),

@@ -574,3 +574,34 @@ def steel_block_3d(Lx=10e-3, Ly=10e-3, Lz=5e-3, h=0.1e-3, fc=5e6, abs_wavelength
                     for y in gy for x in gx]) + 1
     return dict(nds=nds, els=els, el_abs=el_abs, K=K, C=C, M=M, gl=gl, dt=dt,
                 src_nodes=[src + 1], src_dof=3, mon_nodes=mon, mon_dof=3)
+
+
+# ---------------------------------------------------------------------------
+# Element data for adjoint gradients
+
+def cpe3_element_data(nds, els, el_abs, D, rho, gl, dof_to_use=(1, 2), damping_power_law=3,
+                      max_damping=3.1415e7, max_stiffness_reduction=0.01):
+    """Per-element data of a CPE3 model for bfe_adjoint_gradient: stiffness at
+    unit scale with the absorbing grading, lumped mass and damping per unit
+    density (fn_build_global_matrices_v5.m:115-116), 0-based global rows."""
+    K, _, M, ln, ld = cpe3(nds, els, D, rho, list(dof_to_use))
+    a = np.asarray(el_abs, float)
+    K = K * np.exp(np.log(max_stiffness_reduction) * a ** (damping_power_law + 1))[:, None, None]
+    mh = np.einsum("eii->ei", M) / rho
+    ch = mh * (a ** damping_power_law * max_damping)[:, None]
+    dof = gl[els[:, ln - 1] - 1, ld - 1] - 1
+    return K, mh, ch, dof
+
+
+def assemble_from_elements(ke, mh, ch, dof, n, s=None, rho=None):
+    """K = sum s_e K_e, M = diag(sum rho_e Mh_e), C = diag(sum rho_e Ch_e)."""
+    n_el, ndf = dof.shape
+    s = np.ones(n_el) if s is None else np.asarray(s, float)
+    rho = np.ones(n_el) if rho is None else np.asarray(rho, float)
+    r = np.repeat(dof, ndf, axis=1).ravel()
+    c = np.tile(dof, (1, ndf)).ravel()
+    K = sp.csr_matrix(((ke * s[:, None, None]).transpose(0, 2, 1).ravel(), (r, c)), shape=(n, n))
+    K.sum_duplicates()
+    m = np.bincount(dof.ravel(), (mh * rho[:, None]).ravel(), minlength=n)
+    cc = np.bincount(dof.ravel(), (ch * rho[:, None]).ravel(), minlength=n)
+    return K, sp.diags(cc).tocsr(), sp.diags(m).tocsr()

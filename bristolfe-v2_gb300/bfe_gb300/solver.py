@@ -231,6 +231,47 @@ class Plan:
         check(st)
         return hist
 
+    def adjoint_gradient(self, element_data, time, forcing_indices_per_source, forcing_functions,
+                         history_indices, observed, ckpt_every=0, return_history=False):
+        """Misfit J and its gradients w.r.t. per-element stiffness scale and
+        density (adjoint with checkpointing). element_data = (ke, mh, ch, dof)
+        with dof 0-based global rows (n_el x ndf, -1 unused); indices 1-based;
+        observed (q, n_t, R). Returns (J, g_stiff, g_rho[, hist])."""
+        ke, mh, ch, dof = element_data
+        ke = np.ascontiguousarray(ke, np.float64)
+        mh = np.ascontiguousarray(mh, np.float64)
+        ch = np.ascontiguousarray(ch, np.float64)
+        dof = np.ascontiguousarray(dof, np.int64)
+        n_el, ndf = dof.shape
+        time = np.ascontiguousarray(np.asarray(time, float).ravel())
+        nt = time.size
+        R = len(forcing_indices_per_source)
+        p = max(len(np.ravel(x)) for x in forcing_indices_per_source)
+        fi = np.full((p, R), -1, np.int64, order="F")
+        for r, x in enumerate(forcing_indices_per_source):
+            x = np.asarray(x, np.int64).ravel() - 1
+            fi[: x.size, r] = x
+        F = np.asarray(forcing_functions, float)
+        if F.ndim == 1:
+            F = F[None, :]
+        if F.ndim == 2:
+            F = np.repeat(F[:, :nt, None], R, axis=2)
+        F = np.asfortranarray(F[:, :nt, :])
+        hi = np.ascontiguousarray(np.asarray(history_indices, np.int64).ravel() - 1)
+        obs = np.asfortranarray(np.asarray(observed, float))
+        J = ctypes.c_double()
+        gs = np.zeros(n_el)
+        gr = np.zeros(n_el)
+        hist = np.zeros((hi.size, nt, R), order="F")
+        st = self._lib.bfe_adjoint_gradient(
+            self._h, n_el, ndf, ptr(dof, ctypes.c_int64), ptr(ke, ctypes.c_double),
+            ptr(mh, ctypes.c_double), ptr(ch, ctypes.c_double), R, nt, ptr(time, ctypes.c_double),
+            p, ptr(fi, ctypes.c_int64), F.shape[0], ptr(F, ctypes.c_double), hi.size,
+            ptr(hi, ctypes.c_int64), ptr(obs, ctypes.c_double), int(ckpt_every), ctypes.byref(J),
+            ptr(gs, ctypes.c_double), ptr(gr, ctypes.c_double), ptr(hist, ctypes.c_double))
+        check(st)
+        return (J.value, gs, gr, hist) if return_history else (J.value, gs, gr)
+
     def run_device(self, R, n_t, ti_start, frc_dof, frc_rhs, frc_sig, frc_w, d_sig, hist_idx,
                    d_hist, stream=0):
         """Device-resident march: d_sig / d_hist are torch CUDA tensors (FP64).

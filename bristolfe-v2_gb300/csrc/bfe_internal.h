@@ -137,6 +137,26 @@ cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t 
 cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
 cudaError_t launch_advance(int64_t* ti_dev, int64_t k, cudaStream_t s);
 
+// Element data and states of one adjoint gradient contraction (bfe_adjoint.cu).
+struct GradArgs {
+  int64_t n_el;
+  int ndf;                    // DOFs per element (3, 6, 8, 9 or 24)
+  const int32_t* el_dof;      // n_el x ndf global rows (-1 = unused)
+  const void* ke;             // n_el x ndf x ndf unit-scale stiffness (plan precision)
+  const void* mh;             // n_el x ndf lumped mass per unit density
+  const void* ch;             // n_el x ndf damping per unit density
+  const void* lam;            // lam_t   [n][R]
+  const void* u0;             // u_t     [n][R]
+  const void* u1;             // u_{t-1} [n][R]
+  const void* u2;             // u_{t-2} [n][R]
+  int R;
+  double dt;
+  double* gs;                 // dJ/ds   accumulators (n_el)
+  double* gr;                 // dJ/drho accumulators (n_el)
+};
+bool grad_ndf_supported(int ndf);
+cudaError_t launch_grad(const GradArgs& g, int precision, cudaStream_t s);
+
 // Message returned by bfe_last_error() on the calling thread.
 void set_last_error(const char* msg);
 

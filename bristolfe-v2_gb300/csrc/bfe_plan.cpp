@@ -919,18 +919,28 @@ struct RunSpec {
   const double* time = nullptr;    // host time samples (for frame times)
 };
 
-int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
-  const int64_t n = pl->n, R = rs.R;
+// Device arrays of one run (forcing, monitors, per-row info, FP32 signals,
+// interface staging) and the StepArgs template; the states are set per step.
+struct RunArrays {
+  DevBuf<int32_t> frow, frhs, fsig, mrow, mslot;
+  DevBuf<unsigned char> fcoef, vint;
+  DevBuf<uint32_t> info;
+  DevBuf<float> sig32;
+};
+
+int prepare_run(bfe_plan* pl, std::vector<ForceEntry>& frc, const std::vector<int64_t>& hist_idx,
+                int64_t R, int64_t n_t, int64_t n_sig, const double* d_sig64, double* d_hist,
+                cudaStream_t st, RunArrays& ra, bfe::StepArgs& a) {
+  const int64_t n = pl->n;
   const int prec = pl->prec;
   const size_t es = elem_size(prec);
-  if ((double)n * (double)R > 4.0e12) return fail(BFE_ERR_ARG, "state too large");
   // forcing list sorted by (row, rhs)
-  std::sort(rs.frc.begin(), rs.frc.end(), [](const ForceEntry& a, const ForceEntry& b) {
-    return a.row != b.row ? a.row < b.row : a.rhs < b.rhs;
+  std::sort(frc.begin(), frc.end(), [](const ForceEntry& x, const ForceEntry& y) {
+    return x.row != y.row ? x.row < y.row : x.rhs < y.rhs;
   });
   std::vector<int32_t> frow, frhs, fsig;
   std::vector<unsigned char> fcoef;
-  for (auto& f : rs.frc) {
+  for (auto& f : frc) {
     frow.push_back(f.row);
     frhs.push_back(f.rhs);
     fsig.push_back(f.sig);
@@ -939,46 +949,35 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   }
   // monitors sorted by row
   std::vector<std::pair<int32_t, int32_t>> mons;
-  for (size_t k = 0; k < rs.hist_idx.size(); ++k) mons.emplace_back((int32_t)rs.hist_idx[k], (int32_t)k);
+  for (size_t k = 0; k < hist_idx.size(); ++k) mons.emplace_back((int32_t)hist_idx[k], (int32_t)k);
   std::sort(mons.begin(), mons.end());
   std::vector<int32_t> mrow, mslot;
   for (auto& x : mons) { mrow.push_back(x.first); mslot.push_back(x.second); }
   // per-row info word for this run
   std::vector<uint32_t> info(pl->h_base);
-  for (auto& f : rs.frc) info[f.row] |= bfe::kRowForced;
+  for (auto& f : frc) info[f.row] |= bfe::kRowForced;
   for (auto& x : mons) info[x.first] |= bfe::kRowMonitored;
   for (int32_t r : pl->h_int_row) info[r] |= bfe::kRowInterface;
-
-  DevBuf<int32_t> d_frow, d_frhs, d_fsig, d_mrow, d_mslot;
-  DevBuf<unsigned char> d_fcoef, d_u, d_vint;
-  DevBuf<uint32_t> d_info;
-  DevBuf<float> d_sig32;
-  CUDA_TRY(d_frow.upload(frow));
-  CUDA_TRY(d_frhs.upload(frhs));
-  CUDA_TRY(d_fsig.upload(fsig));
-  CUDA_TRY(d_fcoef.upload(fcoef));
-  CUDA_TRY(d_mrow.upload(mrow));
-  CUDA_TRY(d_mslot.upload(mslot));
-  CUDA_TRY(d_info.upload(info));
-  const void* dsig = rs.d_sig64;
-  if (prec == BFE_PREC_SINGLE && rs.n_sig > 0) {
-    CUDA_TRY(d_sig32.alloc((size_t)rs.n_t * rs.n_sig));
-    CUDA_TRY(bfe::launch_cast_f64_to_f32(rs.d_sig64, d_sig32.p, rs.n_t * rs.n_sig, st));
-    dsig = d_sig32.p;
+  CUDA_TRY(ra.frow.upload(frow));
+  CUDA_TRY(ra.frhs.upload(frhs));
+  CUDA_TRY(ra.fsig.upload(fsig));
+  CUDA_TRY(ra.fcoef.upload(fcoef));
+  CUDA_TRY(ra.mrow.upload(mrow));
+  CUDA_TRY(ra.mslot.upload(mslot));
+  CUDA_TRY(ra.info.upload(info));
+  const void* dsig = d_sig64;
+  if (prec == BFE_PREC_SINGLE && n_sig > 0) {
+    CUDA_TRY(ra.sig32.alloc((size_t)n_t * n_sig));
+    CUDA_TRY(bfe::launch_cast_f64_to_f32(d_sig64, ra.sig32.p, n_t * n_sig, st));
+    dsig = ra.sig32.p;
   }
-  const size_t state_bytes = (size_t)n * R * es;
-  CUDA_TRY(d_u.alloc(3 * state_bytes));
-  CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * state_bytes, st));
-  if (pl->n_int) {
-    CUDA_TRY(d_vint.alloc((size_t)pl->n_int * R * es));
-  }
+  if (pl->n_int) CUDA_TRY(ra.vint.alloc((size_t)pl->n_int * R * es));
   if (R > 1) {
     const size_t smem = bfe::batched_smem_bytes(prec, pl->max_slice_entries);
     if (smem > 227 * 1024) return fail(BFE_ERR_UNSUPPORTED, "operator rows too long for the batched kernel");
     CUDA_TRY(bfe::set_batched_smem_limit(prec, std::max<size_t>(smem, 1)));
   }
-
-  bfe::StepArgs a{};
+  a = bfe::StepArgs{};
   a.n = (int32_t)n;
   a.R = (int32_t)R;
   a.n_slices = pl->n_slices;
@@ -986,27 +985,43 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   a.col = pl->col.p;
   a.val = pl->val.p;
   a.rowc = pl->rowc.p;
-  a.rowinfo = d_info.p;
+  a.rowinfo = ra.info.p;
   a.n_frc = (int32_t)frow.size();
-  a.frc_row = d_frow.p;
-  a.frc_rhs = d_frhs.p;
-  a.frc_sig = d_fsig.p;
-  a.frc_coef = d_fcoef.p;
+  a.frc_row = ra.frow.p;
+  a.frc_rhs = ra.frhs.p;
+  a.frc_sig = ra.fsig.p;
+  a.frc_coef = ra.fcoef.p;
   a.sig = dsig;
-  a.n_sig = (int32_t)rs.n_sig;
+  a.n_sig = (int32_t)n_sig;
   a.n_mon = (int32_t)mrow.size();
-  a.mon_row = d_mrow.p;
-  a.mon_slot = d_mslot.p;
-  a.q = (int32_t)rs.hist_idx.size();
-  a.n_t = rs.n_t;
-  a.hist = rs.d_hist;
+  a.mon_row = ra.mrow.p;
+  a.mon_slot = ra.mslot.p;
+  a.q = (int32_t)hist_idx.size();
+  a.n_t = n_t;
+  a.hist = d_hist;
   a.n_int = pl->n_int;
   a.int_row = pl->int_row.p;
   a.z_ptr = pl->z_ptr.p;
   a.z_col = pl->z_col.p;
   a.z_val = pl->z_val.p;
   a.int_base_prev = pl->int_base_prev;
-  a.v_int = d_vint.p;
+  a.v_int = ra.vint.p;
+  return BFE_OK;
+}
+
+int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
+  const int64_t n = pl->n, R = rs.R;
+  const int prec = pl->prec;
+  const size_t es = elem_size(prec);
+  if ((double)n * (double)R > 4.0e12) return fail(BFE_ERR_ARG, "state too large");
+  RunArrays ra;
+  bfe::StepArgs a;
+  int prc = prepare_run(pl, rs.frc, rs.hist_idx, R, rs.n_t, rs.n_sig, rs.d_sig64, rs.d_hist, st, ra, a);
+  if (prc) return prc;
+  DevBuf<unsigned char> d_u;
+  const size_t state_bytes = (size_t)n * R * es;
+  CUDA_TRY(d_u.alloc(3 * state_bytes));
+  CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * state_bytes, st));
   unsigned char* U[3] = {d_u.p, d_u.p + state_bytes, d_u.p + 2 * state_bytes};
   int iprev = 0, icur = 1, inew = 2;
   bfe_stats& stt = pl->last;
@@ -1383,6 +1398,208 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
   rs.d_sig64 = d_sig;
   rs.d_hist = d_hist;
   return execute(plan, rs, static_cast<cudaStream_t>(stream));
+}
+
+// Adjoint gradient of an A-scan misfit with sqrt(N)-step checkpointing (see
+// include/bfe_gb300.h). Forward march with checkpoints of (u_{t-2}, u_{t-1})
+// every c steps and the monitored history; residuals and misfit on the host
+// in FP64; backward sweep over segments: recompute the segment's states from
+// its checkpoint, then step the adjoint (the same operator, driven by the
+// residuals) backwards through the segment and contract each step into the
+// per-element gradient accumulators.
+int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t* el_dof,
+                         const double* ke, const double* mh, const double* ch,
+                         int64_t R, int64_t n_t, const double* time,
+                         int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+                         int64_t q, const int64_t* hist_idx, const double* observed,
+                         int64_t ckpt_every, double* misfit, double* g_stiff, double* g_rho,
+                         double* hist_out) {
+  g_last_error.clear();
+  if (!pl) return fail(BFE_ERR_ARG, "plan is NULL");
+  if (pl->mode != BFE_MODE_VEL_CURRENT)
+    return fail(BFE_ERR_UNSUPPORTED, "the adjoint is defined for 'vel at curent time step'");
+  if (n_el < 1 || !bfe::grad_ndf_supported(ndf) || !el_dof || !ke || !mh || !ch)
+    return fail(BFE_ERR_ARG, "invalid element data (ndf must be 3, 6, 8, 9 or 24)");
+  if (R < 1 || q < 1 || !hist_idx || !observed || !misfit || !g_stiff || !g_rho)
+    return fail(BFE_ERR_ARG, "invalid sizes or NULL outputs");
+  int rc;
+  if ((rc = check_time(pl, n_t, time))) return rc;
+  for (int64_t k = 0; k < q; ++k)
+    if (hist_idx[k] < 0 || hist_idx[k] >= pl->n) return fail(BFE_ERR_ARG, "history index out of range");
+  for (int64_t k = 0; k < n_el * ndf; ++k)
+    if (el_dof[k] < -1 || el_dof[k] >= pl->n) return fail(BFE_ERR_ARG, "element DOF %lld out of range", (long long)k);
+  std::vector<ForceEntry> frc;
+  if ((rc = build_forcing(pl, R, p, frc_idx, frc_rows, frc))) return rc;
+  if (p > 0 && !frcs) return fail(BFE_ERR_ARG, "frcs is NULL");
+  const int64_t ti0 = p > 0 ? first_nonzero_column(frcs, frc_rows, n_t, R) : n_t;
+  const int prec = pl->prec;
+  const size_t es = elem_size(prec);
+  const int64_t n = pl->n;
+  const double dt = pl->dt;
+  cudaStream_t st = pl->stream;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != pl->device) CUDA_TRY(cudaSetDevice(pl->device));
+  *misfit = 0.0;
+  std::fill(g_stiff, g_stiff + n_el, 0.0);
+  std::fill(g_rho, g_rho + n_el, 0.0);
+  if (ti0 >= n_t) return BFE_OK;
+  const int64_t steps = n_t - ti0;
+  const int64_t c = ckpt_every > 0 ? ckpt_every : (int64_t)std::ceil(std::sqrt((double)steps));
+  const int64_t n_seg = (steps + c - 1) / c;
+
+  // element data on the device
+  DevBuf<int32_t> d_dof;
+  DevBuf<unsigned char> d_ke, d_mh, d_ch;
+  {
+    std::vector<int32_t> hd(el_dof, el_dof + n_el * ndf);
+    CUDA_TRY(d_dof.upload(hd));
+    std::vector<unsigned char> b1, b2, b3;
+    for (int64_t k = 0; k < n_el * ndf * ndf; ++k)
+      prec == BFE_PREC_DOUBLE ? push_val<double>(b1, ke[k]) : push_val<float>(b1, ke[k]);
+    for (int64_t k = 0; k < n_el * ndf; ++k) {
+      prec == BFE_PREC_DOUBLE ? push_val<double>(b2, mh[k]) : push_val<float>(b2, mh[k]);
+      prec == BFE_PREC_DOUBLE ? push_val<double>(b3, ch[k]) : push_val<float>(b3, ch[k]);
+    }
+    CUDA_TRY(d_ke.upload(b1));
+    CUDA_TRY(d_mh.upload(b2));
+    CUDA_TRY(d_ch.upload(b3));
+  }
+  // forward inputs
+  const int64_t n_sig = frc_rows * R;
+  DevBuf<double> d_sig, d_hist;
+  {
+    std::vector<double> h((size_t)n_t * n_sig);
+    for (int64_t r = 0; r < R; ++r)
+      for (int64_t ti = 0; ti < n_t; ++ti)
+        for (int64_t k = 0; k < frc_rows; ++k)
+          h[(size_t)ti * n_sig + k + frc_rows * r] = frcs[k + frc_rows * (ti + n_t * r)];
+    CUDA_TRY(d_sig.upload(h));
+  }
+  const size_t hist_n = (size_t)q * n_t * R;
+  CUDA_TRY(d_hist.alloc(hist_n));
+  CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
+  std::vector<int64_t> hidx(hist_idx, hist_idx + q);
+  RunArrays rf;
+  bfe::StepArgs af;
+  if ((rc = prepare_run(pl, frc, hidx, R, n_t, n_sig, d_sig.p, d_hist.p, st, rf, af))) return rc;
+  const bool use_groups = R % 64 == 0 && pl->have_groups && prec == BFE_PREC_SINGLE;
+  const bfe::GroupArgs* grp = use_groups ? &pl->groups : nullptr;
+  auto step = [&](bfe::StepArgs& a) -> int {
+    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
+                           : bfe::launch_step_batched(a, nullptr, grp, prec, pl->max_slice_entries,
+                                                      use_groups ? 14 : 0, st);
+    if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
+    if (pl->n_int) {
+      e = bfe::launch_interface_fixup(a, prec, st);
+      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "interface kernel launch failed: %s", cudaGetErrorString(e));
+    }
+    return BFE_OK;
+  };
+  const size_t sb = (size_t)n * R * es;
+  DevBuf<unsigned char> d_u, d_ck;
+  CUDA_TRY(d_u.alloc(3 * sb));
+  CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * sb, st));
+  CUDA_TRY(d_ck.alloc(2 * sb * n_seg));
+  unsigned char* U[3] = {d_u.p, d_u.p + sb, d_u.p + 2 * sb};
+  int ip = 0, ic = 1, iw = 2;
+  for (int64_t t = ti0; t < n_t; ++t) {
+    if ((t - ti0) % c == 0) {
+      const int64_t j = (t - ti0) / c;
+      CUDA_TRY(cudaMemcpyAsync(d_ck.p + 2 * sb * j, U[ip], sb, cudaMemcpyDeviceToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(d_ck.p + 2 * sb * j + sb, U[ic], sb, cudaMemcpyDeviceToDevice, st));
+    }
+    af.ti = t;
+    af.u_prev = U[ip];
+    af.u_n = U[ic];
+    af.u_new = U[iw];
+    if ((rc = step(af))) return rc;
+    const int tt = ip; ip = ic; ic = iw; iw = tt;
+  }
+  // residuals and misfit (FP64, host)
+  std::vector<double> hist(hist_n);
+  CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (hist_out) std::memcpy(hist_out, hist.data(), hist_n * sizeof(double));
+  const int64_t n_rsig = q * R;
+  std::vector<double> res((size_t)n_t * n_rsig, 0.0);
+  double J = 0.0;
+  for (int64_t r = 0; r < R; ++r)
+    for (int64_t t = ti0; t < n_t; ++t)
+      for (int64_t k = 0; k < q; ++k) {
+        const size_t o = (size_t)k + q * ((size_t)t + n_t * r);
+        const double d = hist[o] - observed[o];
+        J += 0.5 * d * d;
+        res[(size_t)t * n_rsig + k + q * r] = d;
+      }
+  *misfit = J;
+  // adjoint forcing: each receiver of each source driven by its residual,
+  // coefficient A^-1 = (dt^2 / A) / dt^2; repeated receivers add up
+  std::vector<ForceEntry> afrc;
+  for (int64_t r = 0; r < R; ++r)
+    for (int64_t k = 0; k < q; ++k)
+      afrc.push_back({(int32_t)hist_idx[k], (int32_t)r, (int32_t)(k + q * r), 1.0 / (dt * dt)});
+  DevBuf<double> d_res;
+  CUDA_TRY(d_res.upload(res));
+  RunArrays ra;
+  bfe::StepArgs aa;
+  std::vector<int64_t> no_mon;
+  if ((rc = prepare_run(pl, afrc, no_mon, R, n_t, n_rsig, d_res.p, nullptr, st, ra, aa))) return rc;
+  // backward sweep
+  DevBuf<unsigned char> d_seg, d_lam;
+  DevBuf<double> d_gs, d_gr;
+  CUDA_TRY(d_seg.alloc((size_t)(c + 2) * sb));
+  CUDA_TRY(d_lam.alloc(3 * sb));
+  CUDA_TRY(cudaMemsetAsync(d_lam.p, 0, 3 * sb, st));
+  CUDA_TRY(d_gs.alloc(n_el));
+  CUDA_TRY(d_gr.alloc(n_el));
+  CUDA_TRY(cudaMemsetAsync(d_gs.p, 0, n_el * sizeof(double), st));
+  CUDA_TRY(cudaMemsetAsync(d_gr.p, 0, n_el * sizeof(double), st));
+  unsigned char* L[3] = {d_lam.p, d_lam.p + sb, d_lam.p + 2 * sb};
+  int lp = 0, lc = 1, lw = 2;        // lam_{t+2}, lam_{t+1}, lam_t
+  auto S = [&](int64_t k) { return d_seg.p + (size_t)k * sb; };
+  af.n_mon = 0;                      // the recompute does not rewrite the history
+  bfe::GradArgs g{};
+  g.n_el = n_el;
+  g.ndf = ndf;
+  g.el_dof = d_dof.p;
+  g.ke = d_ke.p;
+  g.mh = d_mh.p;
+  g.ch = d_ch.p;
+  g.R = (int)R;
+  g.dt = dt;
+  g.gs = d_gs.p;
+  g.gr = d_gr.p;
+  for (int64_t j = n_seg - 1; j >= 0; --j) {
+    const int64_t ts = ti0 + j * c, te = std::min(ts + c, n_t);
+    CUDA_TRY(cudaMemcpyAsync(S(0), d_ck.p + 2 * sb * j, 2 * sb, cudaMemcpyDeviceToDevice, st));
+    for (int64_t t = ts; t < te; ++t) {
+      af.ti = t;
+      af.u_prev = S(t - ts);
+      af.u_n = S(t - ts + 1);
+      af.u_new = S(t - ts + 2);
+      if ((rc = step(af))) return rc;
+    }
+    for (int64_t t = te - 1; t >= ts; --t) {
+      aa.ti = t;
+      aa.u_prev = L[lp];
+      aa.u_n = L[lc];
+      aa.u_new = L[lw];
+      if ((rc = step(aa))) return rc;
+      g.lam = L[lw];
+      g.u0 = S(t - ts + 2);
+      g.u1 = S(t - ts + 1);
+      g.u2 = S(t - ts);
+      const cudaError_t e = bfe::launch_grad(g, prec, st);
+      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "gradient kernel launch failed: %s", cudaGetErrorString(e));
+      const int tt = lp; lp = lc; lc = lw; lw = tt;
+    }
+  }
+  CUDA_TRY(cudaMemcpyAsync(g_stiff, d_gs.p, n_el * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(g_rho, d_gr.p, n_el * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (dev != pl->device) cudaSetDevice(dev);
+  return BFE_OK;
 }
 
 }  // extern "C"

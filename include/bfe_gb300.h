@@ -162,6 +162,31 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
                    int64_t q, const int64_t* hist_idx, double* d_hist,
                    void* stream);
 
+/*
+ * Gradient of an A-scan misfit by the discrete adjoint of the march (new: the
+ * reference has no adjoint). For R sources (forcing as bfe_run_batched),
+ * monitored DOFs hist_idx[q] and observed A-scans (q x n_t x R):
+ *   J = 1/2 sum_{k,t,r} (h[k,t,r] - observed[k,t,r])^2
+ * and its derivatives with respect to per-element stiffness scales s_e
+ * (K = sum s_e K_e) and densities rho_e (M = sum rho_e Mh_e, C = sum
+ * rho_e Ch_e), evaluated at s = 1 and the model's densities:
+ *   el_dof  n_el x ndf global rows (0-based, -1 unused), ndf in {3,6,8,9,24}
+ *   ke      n_el x ndf x ndf element stiffness at unit scale (with the
+ *           absorbing grading of fn_build_global_matrices_v5.m:116)
+ *   mh, ch  n_el x ndf element lumped mass and damping per unit density
+ * The forward march stores (u_{t-2}, u_{t-1}) every ckpt_every steps
+ * (0 = ceil(sqrt(steps))), the backward sweep recomputes each segment from
+ * its checkpoint and steps the adjoint through it. Only 'vel at curent time
+ * step' plans. hist_out (optional) receives the forward A-scans.
+ */
+int bfe_adjoint_gradient(bfe_plan* plan, int64_t n_el, int32_t ndf, const int64_t* el_dof,
+                         const double* ke, const double* mh, const double* ch,
+                         int64_t R, int64_t n_t, const double* time,
+                         int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+                         int64_t q, const int64_t* hist_idx, const double* observed,
+                         int64_t ckpt_every, double* misfit, double* g_stiff, double* g_rho,
+                         double* hist_out);
+
 /* Counters of a plan's last run (no reference counterpart; used by the
  * benchmark for its roofline and launch-count figures). */
 typedef struct bfe_stats {

@@ -1,0 +1,138 @@
+"""Adjoint gradient (bfe_adjoint_gradient) against the FP64 oracle adjoint and
+central finite differences (the acceptance check: 1e-3 relative)."""
+import numpy as np
+import pytest
+
+import modelgen
+from bfe_gb300 import model
+from oracle import adjoint as oadj
+from oracle import signals
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bfe():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from bfe_gb300 import build
+    build.build()
+    import bfe_gb300
+    bfe_gb300.load()
+    return bfe_gb300
+
+
+@pytest.fixture(scope="module")
+def problem():
+    """Steel plate with absorbers; observed data from a seeded stiffness
+    perturbation (+-5 %); homogeneous candidate model."""
+    m = modelgen.solid_plate(W=2e-3, H=1e-3, h=0.1e-3, abs_thick=0.3e-3)
+    mod = m["mod"]
+    rho = 8000.0
+    ed = model.cpe3_element_data(mod["nds"], mod["els"], mod["el_abs_i"], modelgen.STEEL["D"], rho, m["gl"])
+    ke, mh, ch, dof = ed
+    n = m["K"].shape[0]
+    nt = 350
+    dt = m["dt"]
+    t = np.arange(nt) * dt
+    sig = signals.gaussian_pulse(t, 5e6, 5)
+    top = m["mon_nds"]
+    srcs1 = [modelgen.gi_of(m["gl"], [m["frc_nd"]], 2), modelgen.gi_of(m["gl"], [top[4]], 2)]
+    hi1 = modelgen.gi_of(m["gl"], top, 2)
+    rng = np.random.default_rng(2)
+    s_true = 1 + 0.05 * np.tanh(rng.standard_normal(len(dof)))
+    rho_e = np.full(len(dof), rho)
+    obs = np.zeros((hi1.size, nt, 2))
+    Kt, Ct, Mt = model.assemble_from_elements(ke, mh, ch, dof, n, s_true, rho_e)
+    for r, fi in enumerate(srcs1):
+        U = oadj.forward(Kt, Mt.diagonal(), Ct.diagonal(), dt, nt, fi - 1, sig[None, :], 0)
+        obs[:, :, r] = U[hi1 - 1]
+    return dict(m=m, ed=ed, n=n, t=t, dt=dt, sig=sig, srcs1=srcs1, hi1=hi1, obs=obs, rho_e=rho_e)
+
+
+def _plan(bfe, P, prec, s=None):
+    ke, mh, ch, dof = P["ed"]
+    K, C, M = model.assemble_from_elements(ke, mh, ch, dof, P["n"], s, P["rho_e"])
+    return bfe.Plan(K, C, M, P["dt"], bfe.VEL_CURRENT, prec, P["m"]["gl"])
+
+
+def _gpu_grad(bfe, P, prec, ckpt=0):
+    ke, mh, ch, dof = P["ed"]
+    with _plan(bfe, P, prec) as plan:
+        return plan.adjoint_gradient((ke, mh, ch, dof), P["t"], P["srcs1"], P["sig"], P["hi1"],
+                                     P["obs"], ckpt_every=ckpt)
+
+
+def test_fp64_adjoint_matches_oracle_adjoint(bfe, problem):
+    P = problem
+    ke, mh, ch, dof = P["ed"]
+    J0, gs0, gr0 = oadj.misfit_and_gradient(ke, mh, ch, dof, P["n"], P["dt"], P["t"].size,
+                                            [s - 1 for s in P["srcs1"]], P["sig"][None, :],
+                                            P["hi1"] - 1, P["obs"], rho_e=P["rho_e"])
+    J1, gs1, gr1 = _gpu_grad(bfe, P, "double")
+    assert abs(J1 - J0) <= 1e-9 * J0
+    assert np.abs(gs1 - gs0).max() <= 1e-8 * np.abs(gs0).max()
+    assert np.abs(gr1 - gr0).max() <= 1e-8 * np.abs(gr0).max()
+
+
+def test_adjoint_matches_central_finite_differences(bfe, problem):
+    P = problem
+    J, gs, gr = _gpu_grad(bfe, P, "double")
+    ke, mh, ch, dof = P["ed"]
+    rng = np.random.default_rng(3)
+    big = np.argsort(-np.abs(gs))[:200]             # elements the A-scans are sensitive to
+    picks = rng.choice(big, 6, replace=False)
+
+    def J_at(s=None, rho=None):
+        K, C, M = model.assemble_from_elements(ke, mh, ch, dof, P["n"], s,
+                                               P["rho_e"] if rho is None else rho)
+        with bfe.Plan(K, C, M, P["dt"], bfe.VEL_CURRENT, "double") as plan:
+            h = plan.run_batched(P["t"], P["srcs1"], P["sig"], P["hi1"])
+        return 0.5 * ((h - P["obs"]) ** 2).sum()
+    for e in picks:
+        eps = 1e-3
+        sp_, sm_ = np.ones(len(dof)), np.ones(len(dof))
+        sp_[e] += eps
+        sm_[e] -= eps
+        fd = (J_at(s=sp_) - J_at(s=sm_)) / (2 * eps)
+        assert abs(gs[e] - fd) <= 1e-3 * abs(fd), (e, gs[e], fd)
+        rp, rm = P["rho_e"].copy(), P["rho_e"].copy()
+        rp[e] *= 1 + eps
+        rm[e] *= 1 - eps
+        fdr = (J_at(rho=rp) - J_at(rho=rm)) / (2 * eps * P["rho_e"][e])
+        assert abs(gr[e] - fdr) <= 1e-3 * abs(fdr), (e, gr[e], fdr)
+
+
+def test_checkpoint_interval_does_not_change_gradient(bfe, problem):
+    a = _gpu_grad(bfe, problem, "double", ckpt=1)
+    b = _gpu_grad(bfe, problem, "double", ckpt=0)
+    c = _gpu_grad(bfe, problem, "double", ckpt=problem["t"].size)
+    for x, y in ((a, b), (c, b)):
+        assert x[0] == pytest.approx(y[0], rel=1e-12)
+        assert np.abs(x[1] - y[1]).max() <= 1e-12 * np.abs(y[1]).max()
+
+
+def test_fp32_adjoint_close_to_fp64(bfe, problem):
+    J64, gs64, gr64 = _gpu_grad(bfe, problem, "double")
+    J32, gs32, gr32 = _gpu_grad(bfe, problem, "single")
+    assert abs(J32 - J64) <= 1e-3 * J64
+    assert np.linalg.norm(gs32 - gs64) <= 1e-3 * np.linalg.norm(gs64)
+    assert np.linalg.norm(gr32 - gr64) <= 1e-3 * np.linalg.norm(gr64)
+
+
+def test_autograd_wrapper_gradient(bfe, problem):
+    import torch
+    from bfe_gb300.autograd import AscanMisfit
+    P = problem
+    ne = len(P["ed"][3])
+    prob = dict(element_data=P["ed"], n=P["n"], dt=P["dt"], time=P["t"], sources=P["srcs1"],
+                signal=P["sig"], monitors=P["hi1"], observed=P["obs"], gl_lookup=P["m"]["gl"])
+    s = torch.ones(ne, dtype=torch.float64, requires_grad=True)
+    rho = torch.tensor(P["rho_e"], requires_grad=True)
+    J = AscanMisfit.apply(s, rho, prob)
+    J.backward()
+    J_ref, gs, gr = _gpu_grad(bfe, P, "double")
+    assert float(J) == pytest.approx(J_ref, rel=1e-12)
+    assert np.allclose(s.grad.numpy(), gs, rtol=1e-10, atol=1e-30)
+    assert np.allclose(rho.grad.numpy(), gr, rtol=1e-10, atol=1e-40)
