@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink the model size (testing only; 1.0 = the benchmark model)")
     ap.add_argument("--n-t", type=int, default=None)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the 3D and adjoint sections (quick runs)")
     ap.add_argument("--subdomains", type=int, default=32,
                     help="steel sub-domain models marched with the coupled model (32 = benchmark)")
     return ap.parse_args()
@@ -360,6 +362,10 @@ def run_ours(args):
     h2d = 8 * n_t * R + 8 * (p_max * R + q)
     d2h = 8 * q * n_t * R
 
+    extra = {}
+    if rank == 0 and not args.no_extra:
+        extra["hex3d_c3"] = hex3d_section(torch, bfe_gb300, model)
+        extra["adjoint_c4"] = adjoint_section(torch, bfe_gb300, model)
     result = None
     if rank == 0:
         cpu = cpu_baseline(main["K"], main["C"], main["M"], dt, t, srcs[r_mid][srcs[r_mid] <= offs[1]],
@@ -398,6 +404,7 @@ def run_ours(args):
             "setup_s": {"model_build": t_build, "plans": t_plan},
             "cpu_baseline": cpu,
         }
+        result.update(extra)
         print(json.dumps(result), flush=True)
     plan32.close()
     plan64.close()
@@ -405,6 +412,110 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+def hex3d_section(torch, bfe_gb300, model):
+    """3D steel block of 8-node bricks (10 x 10 x 5 mm at 0.1 mm, 500,000
+    bricks): one source, 3,000 samples, FP32 and FP64 marches, roofline of
+    the step kernel and the FP32 A-scan error against FP64."""
+    m = model.steel_block_3d()
+    n_t = 3000
+    dt = m["dt"]
+    t = np.arange(n_t) * dt
+    sig = model.toneburst(t, 5e6, 5)
+    fi = model.global_indices(m["gl"], m["src_nodes"][0], 3)
+    hi = model.global_indices(m["gl"], m["mon_nodes"], 3)
+    n = m["K"].shape[0]
+    nnz = m["K"].nnz
+    out = {"n_dof": n, "nnz_K": int(nnz), "samples": n_t, "monitors": int(hi.size)}
+    hists = {}
+    peak, _ = measured_peak_hbm()
+    for prec, b in (("single", 4), ("double", 8)):
+        with bfe_gb300.Plan(m["K"], m["C"], m["M"], dt, bfe_gb300.VEL_CURRENT, prec, m["gl"]) as p:
+            p.run(t[:100], fi, sig[:100], hi)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h, _, _ = p.run(t, fi, sig, hi)
+            el = time.perf_counter() - t0
+            hists[prec] = h
+            p.set_timing(True)
+            p.run(t[:300], fi, sig[:300], hi)
+            st = p.stats()
+        step_ms = st["step_ms"] / max(st["step_launches"], 1)
+        gbs = algorithmic_bytes(nnz, n, 1, 1, hi.size, b) / (step_ms * 1e-3) / 1e9
+        out["fp32" if b == 4 else "fp64"] = {"value": n * n_t / el, "unit": UNIT, "march_s": el,
+                                            "step_kernel_ms": step_ms, "achieved_gbs": gbs,
+                                            "frac_of_measured_hbm": gbs / peak}
+    out["ascan_err_fp32_vs_fp64"] = float(np.abs(hists["single"] - hists["double"]).max() /
+                                          np.abs(hists["double"]).max())
+    return out
+
+
+def adjoint_section(torch, bfe_gb300, model, n_fd=20):
+    """Adjoint gradient on the 30 x 15 mm steel plate at 0.05 mm (~360k
+    triangles): 16 sources x 16 receivers, 4,000 samples, observed A-scans
+    from a seeded +-5 % stiffness perturbation (1 mm Gaussian bumps),
+    gradient of the misfit w.r.t. per-element stiffness scale and density
+    (sqrt(N) checkpoints) in FP32 and FP64, FP64 central differences on
+    n_fd random elements of the sensitive region."""
+    m = model.steel_plate_adjoint()
+    ke, mh, ch, dof = m["element_data"]
+    n = m["K"].shape[0]
+    n_t = 4000
+    dt = m["dt"]
+    t = np.arange(n_t) * dt
+    sig = model.toneburst(t, 5e6, 5)
+    srcs = [model.global_indices(m["gl"], s_, 2) for s_ in m["src_nodes"]]
+    rec = model.global_indices(m["gl"], m["rec_nodes"], 2)
+    rho_e = np.full(len(dof), m["rho"])
+    Kt, Ct, Mt = model.assemble_from_elements(ke, mh, ch, dof, n, m["s_true"], rho_e)
+    with bfe_gb300.Plan(Kt, Ct, Mt, dt, bfe_gb300.VEL_CURRENT, "double") as p:
+        obs = p.run_batched(t, srcs, sig, rec)
+    K0, C0, M0 = model.assemble_from_elements(ke, mh, ch, dof, n, None, rho_e)
+    res = {"n_dof": n, "elements": int(len(dof)), "sources": len(srcs), "receivers": int(rec.size),
+           "samples": n_t, "checkpoints": int(np.ceil(np.sqrt(n_t)))}
+    grads = {}
+    for prec in ("single", "double"):
+        with bfe_gb300.Plan(K0, C0, M0, dt, bfe_gb300.VEL_CURRENT, prec, m["gl"]) as p:
+            p.adjoint_gradient((ke, mh, ch, dof), t[:200], srcs, sig, rec, obs[:, :200, :])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            J, gs, gr = p.adjoint_gradient((ke, mh, ch, dof), t, srcs, sig, rec, obs)
+            el = time.perf_counter() - t0
+        grads[prec] = (J, gs, gr)
+        res["fp32" if prec == "single" else "fp64"] = {"gradient_s": el, "misfit": J}
+    J64, gs64, gr64 = grads["double"]
+    _, gs32, gr32 = grads["single"]
+    res["fp32_vs_fp64_rel"] = {"stiffness": float(np.linalg.norm(gs32 - gs64) / np.linalg.norm(gs64)),
+                               "density": float(np.linalg.norm(gr32 - gr64) / np.linalg.norm(gr64))}
+    rng = np.random.default_rng(3)
+    sens = np.nonzero(np.abs(gs64) >= 1e-2 * np.abs(gs64).max())[0]
+    picks = rng.choice(sens, min(n_fd, sens.size), replace=False)
+    plan_fd = {}
+
+    def J_at(s=None, rho=None):
+        K, C, M = model.assemble_from_elements(ke, mh, ch, dof, n, s, rho_e if rho is None else rho)
+        with bfe_gb300.Plan(K, C, M, dt, bfe_gb300.VEL_CURRENT, "double") as p:
+            h = p.run_batched(t, srcs, sig, rec)
+        return 0.5 * ((h - obs) ** 2).sum()
+    t0 = time.perf_counter()
+    errs_s, errs_r = [], []
+    for e in picks:
+        eps = 1e-3
+        sp_, sm_ = np.ones(len(dof)), np.ones(len(dof))
+        sp_[e] += eps
+        sm_[e] -= eps
+        fd = (J_at(s=sp_) - J_at(s=sm_)) / (2 * eps)
+        errs_s.append(abs(gs64[e] - fd) / abs(fd))
+        rp, rm = rho_e.copy(), rho_e.copy()
+        rp[e] *= 1 + eps
+        rm[e] *= 1 - eps
+        fdr = (J_at(rho=rp) - J_at(rho=rm)) / (2 * eps * rho_e[e])
+        errs_r.append(abs(gr64[e] - fdr) / abs(fdr))
+    res["finite_difference"] = {"elements": int(len(picks)), "max_rel_err_stiffness": float(max(errs_s)),
+                                "max_rel_err_density": float(max(errs_r)), "seconds": time.perf_counter() - t0,
+                                "selection": "random elements with |dJ/ds| >= 1e-2 max"}
+    return res
 
 
 def cpu_baseline(K, C, M, dt, t, src_gi, sig, mons, target_s=10.0):

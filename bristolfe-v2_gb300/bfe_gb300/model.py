@@ -605,3 +605,42 @@ def assemble_from_elements(ke, mh, ch, dof, n, s=None, rho=None):
     m = np.bincount(dof.ravel(), (mh * rho[:, None]).ravel(), minlength=n)
     cc = np.bincount(dof.ravel(), (ch * rho[:, None]).ravel(), minlength=n)
     return K, sp.diags(cc).tocsr(), sp.diags(m).tocsr()
+
+
+def steel_plate_adjoint(W=30e-3, H=15e-3, h=0.05e-3, fc=5e6, n_src=16, n_rec=16, abs_wavelengths=3.0,
+                        damping_power_law=3, seed=2, bump_width=1e-3, n_bumps=12, amplitude=0.05):
+    """Adjoint benchmark model: steel plate with absorbing layers on the
+    sides and bottom, n_src point sources and n_rec receivers (DOF 2) spread
+    along the top surface inside the absorbers, and a seeded target stiffness
+    field 1 + sum of Gaussian bumps (width bump_width, clipped to
+    +-amplitude) for generating observed A-scans."""
+    nds, els = rect_mesh(0.0, W, 0.0, H, h)
+    D = isotropic_stiffness(STEEL["E"], STEEL["nu"])
+    rho = STEEL["rho"]
+    ctr = centroids(nds, els)
+    cL = np.sqrt(D[0, 0] / rho)
+    thick = min(abs_wavelengths * cL / fc, W / 4, H / 2)
+    inner = np.array([[thick, thick], [W - thick, thick], [W - thick, H + 1.0], [thick, H + 1.0]])
+    el_abs = np.clip(distance_to_polygon(ctr, inner) / thick, 0.0, 1.0)
+    el_abs[points_in_polygon(ctr, inner)] = 0.0
+    ne = els.shape[0]
+    typ = np.full(ne, TYPE_CODES["CPE3"])
+    K, C, M, gl = assemble(nds, els, np.ones(ne, np.int64), el_abs, typ, [dict(D=D, rho=rho)], (1, 2),
+                           damping_power_law=damping_power_law)
+    dt = element_stable_dt(nds, els, D, rho)
+    ed = cpe3_element_data(nds, els, el_abs, D, rho, gl, (1, 2), damping_power_law)
+    rng = np.random.default_rng(seed)
+    cx = rng.uniform(thick, W - thick, n_bumps)
+    cy = rng.uniform(thick, H - 2 * h, n_bumps)
+    amp = rng.uniform(-1.0, 1.0, n_bumps)
+    field = np.zeros(ne)
+    for x0, y0, a0 in zip(cx, cy, amp):
+        field += a0 * np.exp(-((ctr[:, 0] - x0) ** 2 + (ctr[:, 1] - y0) ** 2) / (2 * bump_width ** 2))
+    s_true = 1 + np.clip(amplitude * field, -amplitude, amplitude)
+    top = np.nonzero(np.isclose(nds[:, 1], H))[0]
+    top = top[(nds[top, 0] >= thick) & (nds[top, 0] <= W - thick)]
+    top = top[np.argsort(nds[top, 0])]
+    src = top[np.linspace(0, top.size - 1, n_src).astype(int)] + 1
+    rec = top[np.linspace(0, top.size - 1, n_rec).astype(int)] + 1
+    return dict(nds=nds, els=els, el_abs=el_abs, K=K, C=C, M=M, gl=gl, dt=dt, element_data=ed,
+                s_true=s_true, rho=rho, src_nodes=[[x] for x in src], rec_nodes=rec)

@@ -133,6 +133,6 @@ def test_autograd_wrapper_gradient(bfe, problem):
     J = AscanMisfit.apply(s, rho, prob)
     J.backward()
     J_ref, gs, gr = _gpu_grad(bfe, P, "double")
-    assert float(J) == pytest.approx(J_ref, rel=1e-12)
+    assert float(J.detach()) == pytest.approx(J_ref, rel=1e-12)
     assert np.allclose(s.grad.numpy(), gs, rtol=1e-10, atol=1e-30)
     assert np.allclose(rho.grad.numpy(), gr, rtol=1e-10, atol=1e-40)
