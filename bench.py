@@ -491,10 +491,21 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20):
     rng = np.random.default_rng(3)
     sens = np.nonzero(np.abs(gs64) >= 1e-2 * np.abs(gs64).max())[0]
     picks = rng.choice(sens, min(n_fd, sens.size), replace=False)
-    plan_fd = {}
 
-    def J_at(s=None, rho=None):
-        K, C, M = model.assemble_from_elements(ke, mh, ch, dof, n, s, rho_e if rho is None else rho)
+    import scipy.sparse as sp
+
+    def element_block(e, vals):
+        """Sparse n x n matrix holding one element's ndf x ndf block."""
+        d = dof[e]
+        ok = d >= 0
+        d = d[ok]
+        v = np.asarray(vals)[np.ix_(ok, ok)] if np.ndim(vals) == 2 else np.diag(np.asarray(vals)[ok])
+        return sp.csr_matrix((v.T.ravel(), (np.repeat(d, d.size), np.tile(d, d.size))), shape=(n, n))
+
+    def J_at(dK=None, dM=None, dC=None):
+        K = K0 if dK is None else (K0 + dK).tocsr()
+        M = M0 if dM is None else (M0 + dM).tocsr()
+        C = C0 if dC is None else (C0 + dC).tocsr()
         with bfe_gb300.Plan(K, C, M, dt, bfe_gb300.VEL_CURRENT, "double") as p:
             h = p.run_batched(t, srcs, sig, rec)
         return 0.5 * ((h - obs) ** 2).sum()
@@ -502,15 +513,12 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20):
     errs_s, errs_r = [], []
     for e in picks:
         eps = 1e-3
-        sp_, sm_ = np.ones(len(dof)), np.ones(len(dof))
-        sp_[e] += eps
-        sm_[e] -= eps
-        fd = (J_at(s=sp_) - J_at(s=sm_)) / (2 * eps)
+        dk = element_block(e, ke[e]) * eps                  # s_e = 1 +- eps
+        fd = (J_at(dK=dk) - J_at(dK=-dk)) / (2 * eps)
         errs_s.append(abs(gs64[e] - fd) / abs(fd))
-        rp, rm = rho_e.copy(), rho_e.copy()
-        rp[e] *= 1 + eps
-        rm[e] *= 1 - eps
-        fdr = (J_at(rho=rp) - J_at(rho=rm)) / (2 * eps * rho_e[e])
+        dm = element_block(e, mh[e]) * (eps * rho_e[e])     # rho_e (1 +- eps)
+        dc = element_block(e, ch[e]) * (eps * rho_e[e])
+        fdr = (J_at(dM=dm, dC=dc) - J_at(dM=-dm, dC=-dc)) / (2 * eps * rho_e[e])
         errs_r.append(abs(gr64[e] - fdr) / abs(fdr))
     res["finite_difference"] = {"elements": int(len(picks)), "max_rel_err_stiffness": float(max(errs_s)),
                                 "max_rel_err_density": float(max(errs_r)), "seconds": time.perf_counter() - t0,
