@@ -23,6 +23,7 @@ BFE_CSR = 0
 BFE_CSC = 1
 BFE_MODE_VEL_CURRENT = 0
 BFE_MODE_VEL_LAST_HALF = 1
+BFE_MODE_V5 = 2
 BFE_PREC_DOUBLE = 0
 BFE_PREC_SINGLE = 1
 
@@ -58,6 +59,8 @@ SIGNATURES = {
     "bfe_plan_ndof": (I32, [VP, PI64]),
     "bfe_run": (I32, [VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, I32, PD, PD, PD]),
     "bfe_run_batched": (I32, [VP, I64, I64, PD, I64, PI64, I64, PD, I64, PI64, PD]),
+    "bfe_run_v5": (I32, [VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, PD, I64, PI64, I64,
+                         PD, PD, PD, PD]),
     "bfe_run_device": (I32, [VP, I64, I64, I64, I64, PI64, PI64, PI64, PD, I64, VP,
                              I64, PI64, VP, VP]),
     "bfe_adjoint_gradient": (I32, [VP, I64, I32, PI64, PD, PD, PD, I64, I64, PD, I64, PI64, I64, PD,

@@ -18,7 +18,9 @@ VEL_LAST_HALF = "vel at last half time step"     # v6.m:131
 VEL_CURRENT = "vel at curent time step"          # v6.m:135 (sic)
 DISP_FIELD_TYPES = ("mean(u1)", "mean(u2)", "mean(u3)", "curl(u)", "div(u)", "raw(u)")  # v6.m:64-69
 
-_MODES = {VEL_CURRENT: _lib.BFE_MODE_VEL_CURRENT, VEL_LAST_HALF: _lib.BFE_MODE_VEL_LAST_HALF}
+V5 = "v5"                                        # fn_explicit_dynamic_solver_v5.m
+_MODES = {VEL_CURRENT: _lib.BFE_MODE_VEL_CURRENT, VEL_LAST_HALF: _lib.BFE_MODE_VEL_LAST_HALF,
+          V5: _lib.BFE_MODE_V5}
 
 
 class SolverError(RuntimeError):
@@ -200,6 +202,60 @@ class Plan:
         check(st)
         return hist, fld, fld_t
 
+    def run_v5(self, time, forcing_indices, forcing_functions, disp_indices, disp_functions,
+               history_indices, field_output_every_n_frames=np.inf):
+        """One load step of the v5 scheme (plan created with solver_mode V5),
+        1-based indices, as fn_explicit_dynamic_solver_v5.m:60-188.
+
+        Returns (hist q x n_t, fld n x n_frames or None, frc r x n_t or None,
+        fld_time or None). Forcing shorter than time keeps its last column
+        (v5.m:145-147); prescribed displacements need n_t columns."""
+        time = np.ascontiguousarray(np.asarray(time, float).ravel())
+        nt = time.size
+        fi = np.ascontiguousarray(np.asarray(forcing_indices, np.int64).ravel() - 1) \
+            if forcing_indices is not None else np.zeros(0, np.int64)
+        p = fi.size
+        F = None
+        rows = 0
+        if p:
+            F = np.atleast_2d(np.asarray(forcing_functions, float))
+            if F.shape[1] == 0:
+                raise SolverError("forcing_functions is empty")
+            if F.shape[1] < nt:
+                F = np.hstack([F, np.repeat(F[:, -1:], nt - F.shape[1], axis=1)])
+            F = np.asfortranarray(F[:, :nt])
+            rows = F.shape[0]
+        di = np.ascontiguousarray(np.asarray(disp_indices, np.int64).ravel() - 1) \
+            if disp_indices is not None else np.zeros(0, np.int64)
+        r = di.size
+        D = None
+        drows = 0
+        frc = None
+        if r:
+            D = np.atleast_2d(np.asarray(disp_functions, float))
+            if D.shape[1] < nt:
+                raise SolverError("disp_functions has fewer columns than time samples")
+            D = np.asfortranarray(D[:, :nt])
+            drows = D.shape[0]
+            frc = np.zeros((r, nt), order="F")
+        hi = np.ascontiguousarray(np.asarray(history_indices, np.int64).ravel() - 1) \
+            if history_indices is not None else np.zeros(0, np.int64)
+        q = hi.size
+        hist = np.zeros((q, nt), order="F")
+        every = 0 if np.isinf(field_output_every_n_frames) else int(field_output_every_n_frames)
+        fld = fld_t = None
+        if every > 0:
+            nf = (nt + every - 1) // every
+            fld = np.zeros((self.n, nf), order="F")
+            fld_t = np.zeros(nf)
+        st = self._lib.bfe_run_v5(self._h, nt, ptr(time, ctypes.c_double), p, ptr(fi, ctypes.c_int64),
+                                  rows, ptr(F, ctypes.c_double), r, ptr(di, ctypes.c_int64), drows,
+                                  ptr(D, ctypes.c_double), q, ptr(hi, ctypes.c_int64), every,
+                                  ptr(hist, ctypes.c_double), ptr(fld, ctypes.c_double),
+                                  ptr(fld_t, ctypes.c_double), ptr(frc, ctypes.c_double))
+        check(st)
+        return hist, fld, frc, fld_t
+
     def run_batched(self, time, forcing_indices_per_source, forcing_functions, history_indices):
         """R load steps sharing this operator as one multi-RHS march.
 
@@ -315,6 +371,9 @@ def fn_explicit_dynamic_solver_gb300(K, C, M, time, forcing_indices, forcing_fun
     if disp_indices is not None and len(np.ravel(disp_indices)):
         raise SolverError("prescribed displacements are not supported by the v6 path "
                           "(the reference reads an undefined u_previous, v6.m:191)")
+    if solver_mode not in (VEL_CURRENT, VEL_LAST_HALF):
+        raise SolverError("unknown solver_mode %r (accepted: %r, %r)"
+                          % (solver_mode, VEL_CURRENT, VEL_LAST_HALF))
     time = np.asarray(time, float).ravel()
     dt = time[1] - time[0]
     is_vel = field_output_type not in DISP_FIELD_TYPES
@@ -324,3 +383,31 @@ def fn_explicit_dynamic_solver_gb300(K, C, M, time, forcing_indices, forcing_fun
     if history_indices is None or len(np.ravel(history_indices)) == 0:
         hist = None
     return hist, fld, None, fld_t
+
+
+def fn_explicit_dynamic_solver_v5_gb300(K, C, M, time, forcing_indices, forcing_functions,
+                                        disp_indices, disp_functions, history_indices,
+                                        field_output_every_n_frames, use_gpu_if_present=1,
+                                        solver_precision="double", gl_lookup=None):
+    """Drop-in for fn_explicit_dynamic_solver_v5 (its 11 arguments, 1-based
+    indices; v5.m:1-5). Returns (history_output, field_output, force_output,
+    field_output_time); the field output is the velocity (v5.m:31,168-177).
+
+    ``solver_precision`` and ``gl_lookup`` are extensions: the reference's v5
+    is FP64 only."""
+    n = K.shape[0]
+    if K.shape[0] != K.shape[1]:
+        raise SolverError("K must be square matrix")                          # v5.m:50-52
+    if C.shape != (n, n):
+        raise SolverError("C must be square matrix, same size as K")          # v5.m:53-55
+    if M.shape != (n, n):
+        raise SolverError("M must be square matrix, same size as K")          # v5.m:56-58
+    time = np.asarray(time, float).ravel()
+    dt = time[1] - time[0]
+    with Plan(K, C, M, dt, V5, solver_precision, gl_lookup) as plan:
+        hist, fld, frc, fld_t = plan.run_v5(time, forcing_indices, forcing_functions, disp_indices,
+                                            disp_functions, history_indices,
+                                            field_output_every_n_frames)
+    if history_indices is None or len(np.ravel(history_indices)) == 0:
+        hist = None
+    return hist, fld, frc, fld_t

@@ -137,6 +137,51 @@ cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t 
 cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
 cudaError_t launch_advance(int64_t* ti_dev, int64_t k, cudaStream_t s);
 
+// Prescribed displacements of the v5 scheme (fn_explicit_dynamic_solver_v5.m
+// :142-188). The main step kernel advances every row with the velocity
+// u_n - u_{n-1}; the v5 kernel then handles the rows that differ from that:
+//  * prescribed DOFs ("slots"): the displacement is overwritten, the velocity
+//    keeps its own dynamic value ud (v5.m:150-156 evaluated at the DOF, in
+//    FP64), and every listed entry writes its reaction force
+//    m accn + K(d,:) u_n (v5.m:161);
+//  * correction rows: rows coupled through off-diagonal C to a prescribed DOF
+//    j, whose damping term used (u_n - u_{n-1})[j] instead of dt ud[j].
+// History and field-frame values of all these rows are written here (they
+// are left out of the step kernels' monitor list).
+struct V5Args {
+  int32_t n_ent;              // listed entries (rows of the force output)
+  const int32_t* ent_row;     // global row of each entry
+  const int32_t* ent_slot;    // slot of the entry's DOF
+  const int32_t* ent_last;    // 1: this entry sets the DOF's displacement
+  const double* dsp;          // [n_t][n_ent] prescribed displacements
+  const double* accn;         // [n_t][n_ent] their second differences / dt^2
+  double* frc_out;            // n_ent x n_t, entry fastest
+  int32_t n_slot;             // distinct prescribed DOFs
+  const int32_t* slot_row;
+  const double* slot_m;       // lumped mass
+  const int32_t* k_ptr;       // K rows of the slots (CSR, FP64)
+  const int32_t* k_col;
+  const double* k_val;
+  const int32_t* c_ptr;       // C rows of the slots (CSR, FP64)
+  const int32_t* c_col;
+  const int32_t* c_cslot;     // slot of each C column if prescribed, else -1
+  const double* c_val;
+  const int32_t* f_sig;       // forcing signal of the slot's DOF (-1: none)
+  const double* f_w;          // and its weight
+  int32_t n_cor;              // correction rows
+  const int32_t* cor_row;
+  const int32_t* cor_ptr;     // per row: entries (prescribed slot, -dt C_ij / m_i)
+  const int32_t* cor_slot;
+  const double* cor_val;
+  const int32_t* h_ptr;       // history slots of slots [0, n_slot) then of
+  const int32_t* h_slot;      // correction rows [n_slot, n_slot + n_cor)
+  const double* ud_old;       // dynamic velocity at the slots, step n
+  double* ud_new;             // and step n + 1
+  double* fld;                // field frame column (n values) or nullptr
+  double dt;
+};
+cudaError_t launch_v5(const StepArgs& a, const V5Args& v, int precision, cudaStream_t s);
+
 // Element data and states of one adjoint gradient contraction (bfe_adjoint.cu).
 struct GradArgs {
   int64_t n_el;

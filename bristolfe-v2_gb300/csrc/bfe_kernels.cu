@@ -907,6 +907,63 @@ __global__ void frame_kernel(StepArgs a, double* fld, int64_t frame, int is_vel,
   fld[(size_t)i + (size_t)a.n * frame] = is_vel ? (un - uo) / dt : un;
 }
 
+// v5 prescribed-displacement rows (V5Args): one thread per listed entry,
+// then one per correction row. Reads u_n, u_{n-1} and ud_old, writes u_new
+// at prescribed and correction rows only (disjoint), ud_new and frc_out.
+template <typename T>
+__global__ void __launch_bounds__(128) v5_kernel(StepArgs a, V5Args v) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const T* un = static_cast<const T*>(a.u_n);
+  const T* up = static_cast<const T*>(a.u_prev);
+  T* unew = static_cast<T*>(a.u_new);
+  const int64_t ti = step_index(a);
+  const double dt = v.dt;
+  if (g < v.n_ent) {
+    const int s = __ldg(v.ent_slot + g);
+    double ku = 0.0;
+    for (int e = __ldg(v.k_ptr + s); e < __ldg(v.k_ptr + s + 1); ++e)
+      ku = fma(__ldg(v.k_val + e), (double)un[__ldg(v.k_col + e)], ku);
+    const double m = __ldg(v.slot_m + s);
+    v.frc_out[(size_t)g + (size_t)v.n_ent * ti] = m * __ldg(v.accn + (size_t)ti * v.n_ent + g) + ku;
+    if (!__ldg(v.ent_last + g)) return;
+    // udd = (f - K u - C ud) / m  (v5.m:150), ud += dt udd  (v5.m:153)
+    double cv = 0.0;
+    for (int e = __ldg(v.c_ptr + s); e < __ldg(v.c_ptr + s + 1); ++e) {
+      const int k = __ldg(v.c_col + e);
+      const int ks = __ldg(v.c_cslot + e);
+      const double udk = ks >= 0 ? v.ud_old[ks] : ((double)un[k] - (double)up[k]) / dt;
+      cv = fma(__ldg(v.c_val + e), udk, cv);
+    }
+    double f = 0.0;
+    const int fs = __ldg(v.f_sig + s);
+    if (fs >= 0) f = __ldg(v.f_w + s) * (double)static_cast<const T*>(a.sig)[(size_t)ti * a.n_sig + fs];
+    const double ud = v.ud_old[s] + dt * ((f - ku - cv) / m);
+    v.ud_new[s] = ud;
+    const int row = __ldg(v.ent_row + g);
+    const T u = (T)__ldg(v.dsp + (size_t)ti * v.n_ent + g);
+    unew[row] = u;
+    for (int h = __ldg(v.h_ptr + s); h < __ldg(v.h_ptr + s + 1); ++h)
+      a.hist[(size_t)__ldg(v.h_slot + h) + (size_t)a.q * (size_t)ti] = (double)u;
+    if (v.fld) v.fld[row] = ud;
+    return;
+  }
+  const int t = g - v.n_ent;
+  if (t >= v.n_cor) return;
+  const int row = __ldg(v.cor_row + t);
+  double corr = 0.0;
+  for (int e = __ldg(v.cor_ptr + t); e < __ldg(v.cor_ptr + t + 1); ++e) {
+    const int s = __ldg(v.cor_slot + e);
+    const int j = __ldg(v.slot_row + s);
+    corr = fma(__ldg(v.cor_val + e), dt * v.ud_old[s] - ((double)un[j] - (double)up[j]), corr);
+  }
+  const T u = (T)((double)unew[row] + corr);
+  unew[row] = u;
+  const int hs = v.n_slot + t;
+  for (int h = __ldg(v.h_ptr + hs); h < __ldg(v.h_ptr + hs + 1); ++h)
+    a.hist[(size_t)__ldg(v.h_slot + h) + (size_t)a.q * (size_t)ti] = (double)u;
+  if (v.fld) v.fld[row] = ((double)u - (double)un[row]) / dt;
+}
+
 __global__ void advance_kernel(int64_t* ti_dev, int64_t k) { *ti_dev += k; }
 
 __global__ void cast_kernel(const double* in, float* out, int64_t n) {
@@ -1037,6 +1094,16 @@ cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t 
   const int blocks = (a.n + threads - 1) / threads;
   if (precision == 0) frame_kernel<double><<<blocks, threads, 0, st>>>(a, fld, frame, field_is_vel, dt);
   else frame_kernel<float><<<blocks, threads, 0, st>>>(a, fld, frame, field_is_vel, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_v5(const StepArgs& a, const V5Args& v, int precision, cudaStream_t st) {
+  const int total = v.n_ent + v.n_cor;
+  if (total == 0) return cudaSuccess;
+  const int threads = 128;
+  const int blocks = (total + threads - 1) / threads;
+  if (precision == 0) v5_kernel<double><<<blocks, threads, 0, st>>>(a, v);
+  else v5_kernel<float><<<blocks, threads, 0, st>>>(a, v);
   return cudaGetLastError();
 }
 

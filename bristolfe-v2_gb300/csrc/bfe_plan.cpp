@@ -267,6 +267,10 @@ struct bfe_plan {
   DevBuf<int> d_err;
   bfe::TmaArgs tma{};
   DevBuf<float> g_coef[bfe::kMaxGroups];
+  // BFE_MODE_V5: K, C (FP64 CSR) and the lumped mass, for the
+  // prescribed-displacement rows of bfe_run_v5
+  Csr hK, hC;
+  std::vector<double> h_m;
   bfe::NodeArgs node_args() const {
     bfe::NodeArgs g{};
     g.n_nodes = n_nodes;
@@ -402,7 +406,8 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   g_last_error.clear();
   if (!out) return fail(BFE_ERR_ARG, "out is NULL");
   *out = nullptr;
-  if (solver_mode != BFE_MODE_VEL_CURRENT && solver_mode != BFE_MODE_VEL_LAST_HALF)
+  if (solver_mode != BFE_MODE_VEL_CURRENT && solver_mode != BFE_MODE_VEL_LAST_HALF &&
+      solver_mode != BFE_MODE_V5)
     return fail(BFE_ERR_ARG, "unknown solver_mode %d", solver_mode);
   if (precision != BFE_PREC_DOUBLE && precision != BFE_PREC_SINGLE)
     return fail(BFE_ERR_ARG, "unknown precision %d", precision);
@@ -791,6 +796,11 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
     if ((rc = upload_bytes(pl->z_val, zv))) return rc;
   }
   CUDA_TRY(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
+  if (solver_mode == BFE_MODE_V5) {
+    pl->hK = std::move(K);
+    pl->hC = std::move(C);
+    pl->h_m = m;
+  }
   *out = pl.release();
   return BFE_OK;
 }
@@ -917,6 +927,8 @@ struct RunSpec {
   double* d_fld = nullptr;
   std::vector<double>* fld_time = nullptr;
   const double* time = nullptr;    // host time samples (for frame times)
+  const bfe::V5Args* v5 = nullptr; // prescribed-displacement rows (bfe_run_v5)
+  double* d_ud[2] = {nullptr, nullptr};
 };
 
 // Device arrays of one run (forcing, monitors, per-row info, FP32 signals,
@@ -949,7 +961,8 @@ int prepare_run(bfe_plan* pl, std::vector<ForceEntry>& frc, const std::vector<in
   }
   // monitors sorted by row
   std::vector<std::pair<int32_t, int32_t>> mons;
-  for (size_t k = 0; k < hist_idx.size(); ++k) mons.emplace_back((int32_t)hist_idx[k], (int32_t)k);
+  for (size_t k = 0; k < hist_idx.size(); ++k)
+    if (hist_idx[k] >= 0) mons.emplace_back((int32_t)hist_idx[k], (int32_t)k);   // < 0: written elsewhere
   std::sort(mons.begin(), mons.end());
   std::vector<int32_t> mrow, mslot;
   for (auto& x : mons) { mrow.push_back(x.first); mslot.push_back(x.second); }
@@ -1006,6 +1019,10 @@ int prepare_run(bfe_plan* pl, std::vector<ForceEntry>& frc, const std::vector<in
   a.z_val = pl->z_val.p;
   a.int_base_prev = pl->int_base_prev;
   a.v_int = ra.vint.p;
+  // uploads (here and by the caller before this point) use cudaMemcpy on the
+  // legacy stream, which for pageable memory may return before its DMA lands;
+  // the run's non-blocking stream does not wait for it
+  CUDA_TRY(cudaStreamSynchronize(cudaStreamLegacy));
   return BFE_OK;
 }
 
@@ -1111,7 +1128,8 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     }
   }
   stt.variant = variant;
-  // One time step: step kernel, interface correction, optional frame.
+  int v5_flip = 0;
+  // One time step: step kernel, interface correction, optional frame, v5 rows.
   auto one_step = [&](int64_t ti, bool rec) -> int {
     a.u_prev = U[iprev];
     a.u_n = U[icur];
@@ -1128,6 +1146,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       if (rec && timing) CUDA_TRY(mark(ev_aux));
       stt.aux_launches++;
     }
+    double* frame_col = nullptr;
     if (ti >= 0 && rs.every_n > 0 && rs.d_fld && ti % rs.every_n == 0) {
       const int64_t k = ti / rs.every_n;
       if (rec && timing) CUDA_TRY(mark(ev_aux));
@@ -1136,6 +1155,19 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       if (rec && timing) CUDA_TRY(mark(ev_aux));
       stt.aux_launches++;
       if (rs.fld_time) (*rs.fld_time)[k] = rs.time[ti];
+      frame_col = rs.d_fld + (size_t)n * k;
+    }
+    if (rs.v5) {
+      bfe::V5Args v = *rs.v5;
+      v.ud_old = rs.d_ud[v5_flip];
+      v.ud_new = rs.d_ud[v5_flip ^ 1];
+      v.fld = frame_col;
+      v5_flip ^= 1;
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
+      e = bfe::launch_v5(a, v, prec, st);
+      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "v5 kernel launch failed: %s", cudaGetErrorString(e));
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
+      stt.aux_launches++;
     }
     const int t = iprev;
     iprev = icur;
@@ -1145,7 +1177,8 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   };
   int64_t ti = rs.ti_start;
   // CUDA graph replay: the launches of kGraphSteps consecutive steps (a
-  // multiple of the 3-buffer rotation) are captured once, with the time index
+  // multiple of the 3-buffer state rotation and of the 2-buffer v5 velocity
+  // swap) are captured once, with the time index
   // read from a device counter that the last node advances, and replayed.
   // Not used with per-launch timing, field frames or the legacy stream.
   const int64_t kGraphSteps = 48;
@@ -1361,6 +1394,229 @@ int bfe_run(bfe_plan* plan, int64_t n_t, const double* time,
   CUDA_TRY(cudaMemcpyAsync(fld_out, d_fld.p, (size_t)plan->n * n_frames * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
+  if (dev != plan->device) cudaSetDevice(dev);
+  return BFE_OK;
+}
+
+int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,
+               int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+               int64_t r, const int64_t* dsp_idx, int64_t dsp_rows, const double* dsps,
+               int64_t q, const int64_t* hist_idx, int64_t every_n,
+               double* hist_out, double* fld_out, double* fld_time_out, double* frc_out) {
+  g_last_error.clear();
+  if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
+  if (plan->mode != BFE_MODE_V5) return fail(BFE_ERR_ARG, "the plan was not created with BFE_MODE_V5");
+  int rc;
+  if ((rc = check_time(plan, n_t, time))) return rc;
+  if (q < 0 || p < 0 || r < 0) return fail(BFE_ERR_ARG, "negative sizes");
+  if (p > 0 && !frcs) return fail(BFE_ERR_ARG, "frcs is NULL");
+  if (q > 0 && (!hist_idx || !hist_out)) return fail(BFE_ERR_ARG, "hist_idx/hist_out is NULL");
+  if (r > 0 && (!dsp_idx || !dsps || !frc_out)) return fail(BFE_ERR_ARG, "dsp_idx/dsps/frc_out is NULL");
+  if (r > 0 && dsp_rows != r && !(dsp_rows == 1 && r == 1))
+    return fail(BFE_ERR_ARG, "disp_functions must have %lld rows, got %lld", (long long)r, (long long)dsp_rows);
+  if (every_n > 0 && (!fld_out || !fld_time_out)) return fail(BFE_ERR_ARG, "fld_out/fld_time_out is NULL");
+  const int64_t n = plan->n;
+  for (int64_t k = 0; k < q; ++k)
+    if (hist_idx[k] < 0 || hist_idx[k] >= n) return fail(BFE_ERR_ARG, "history index %lld out of range", (long long)hist_idx[k]);
+  for (int64_t e = 0; e < r; ++e)
+    if (dsp_idx[e] < 0 || dsp_idx[e] >= n) return fail(BFE_ERR_ARG, "displacement index %lld out of range", (long long)dsp_idx[e]);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != plan->device) CUDA_TRY(cudaSetDevice(plan->device));
+  RunSpec rs;
+  rs.R = 1;
+  rs.n_t = n_t;
+  rs.time = time;
+  if ((rc = build_forcing(plan, 1, p, frc_idx, frc_rows, rs.frc))) return rc;
+  rs.ti_start = std::min(p > 0 ? first_nonzero_column(frcs, frc_rows, n_t, 1) : n_t,
+                         r > 0 ? first_nonzero_column(dsps, dsp_rows, n_t, 1) : n_t);
+  const double dt = time[1] - time[0];
+
+  // prescribed DOFs: one slot per distinct DOF; the last listed entry sets it
+  std::map<int64_t, int32_t> slot_of;
+  std::vector<int32_t> slot_row, ent_row(r), ent_slot(r), ent_last(r, 0);
+  std::map<int64_t, int64_t> last_ent;
+  for (int64_t e = 0; e < r; ++e) {
+    auto it = slot_of.find(dsp_idx[e]);
+    if (it == slot_of.end()) {
+      it = slot_of.emplace(dsp_idx[e], (int32_t)slot_row.size()).first;
+      slot_row.push_back((int32_t)dsp_idx[e]);
+    }
+    ent_row[e] = (int32_t)dsp_idx[e];
+    ent_slot[e] = it->second;
+    last_ent[dsp_idx[e]] = e;
+  }
+  for (auto& kv : last_ent) ent_last[kv.second] = 1;
+  const int64_t ns = (int64_t)slot_row.size();
+  // displacements and their second differences (two leading zero columns,
+  // v5.m:73-76), time-major; diag_M(d, d) * accn with repeated DOFs sums the
+  // accelerations of every entry of the same DOF (v5.m:161)
+  std::vector<double> hd((size_t)n_t * r), ha((size_t)n_t * r), hsum((size_t)n_t * ns, 0.0);
+  for (int64_t e = 0; e < r; ++e) {
+    const int64_t row = dsp_rows == 1 ? 0 : e;
+    for (int64_t ti = 0; ti < n_t; ++ti) {
+      const double d0 = dsps[row + dsp_rows * ti];
+      const double d1 = ti >= 1 ? dsps[row + dsp_rows * (ti - 1)] : 0.0;
+      const double d2 = ti >= 2 ? dsps[row + dsp_rows * (ti - 2)] : 0.0;
+      hd[(size_t)ti * r + e] = d0;
+      const double acc = (d0 - 2 * d1 + d2) / (dt * dt);
+      hsum[(size_t)ti * ns + ent_slot[e]] += acc;
+    }
+  }
+  for (int64_t e = 0; e < r; ++e)
+    for (int64_t ti = 0; ti < n_t; ++ti) ha[(size_t)ti * r + e] = hsum[(size_t)ti * ns + ent_slot[e]];
+  // K and C rows of the slots, forcing of the slot DOFs
+  std::vector<int32_t> kp(1, 0), kc, cp(1, 0), cc, ccs, fsig(ns, -1);
+  std::vector<double> kv, cv, sm(ns), fw(ns, 0.0);
+  for (int64_t s = 0; s < ns; ++s) {
+    const int64_t i = slot_row[s];
+    for (int64_t e = plan->hK.ptr[i]; e < plan->hK.ptr[i + 1]; ++e) {
+      kc.push_back((int32_t)plan->hK.idx[e]);
+      kv.push_back(plan->hK.val[e]);
+    }
+    kp.push_back((int32_t)kc.size());
+    for (int64_t e = plan->hC.ptr[i]; e < plan->hC.ptr[i + 1]; ++e) {
+      const int64_t j = plan->hC.idx[e];
+      auto it = slot_of.find(j);
+      cc.push_back((int32_t)j);
+      ccs.push_back(it == slot_of.end() ? -1 : it->second);
+      cv.push_back(plan->hC.val[e]);
+    }
+    cp.push_back((int32_t)cc.size());
+    sm[s] = plan->h_m[i];
+  }
+  for (auto& f : rs.frc) {
+    auto it = slot_of.find(f.row);
+    if (it != slot_of.end()) { fsig[it->second] = f.sig; fw[it->second] = f.w; }
+  }
+  // correction rows: C_ij != 0 (i != j) for a prescribed j and free i;
+  // Z_ij = -dt C_ij / m_i is the 'last half' interface coefficient
+  std::map<int64_t, std::vector<std::pair<int32_t, double>>> cor;
+  if (ns) {
+    for (int64_t i = 0; i < n; ++i) {
+      if (slot_of.count(i)) continue;
+      for (int64_t e = plan->hC.ptr[i]; e < plan->hC.ptr[i + 1]; ++e) {
+        auto it = slot_of.find(plan->hC.idx[e]);
+        if (it != slot_of.end() && plan->hC.val[e] != 0.0)
+          cor[i].emplace_back(it->second, -dt * plan->hC.val[e] / plan->h_m[i]);
+      }
+    }
+  }
+  std::vector<int32_t> crow, cptr(1, 0), cslot;
+  std::vector<double> cval;
+  std::map<int64_t, int32_t> cor_of;
+  for (auto& kvp : cor) {
+    cor_of[kvp.first] = (int32_t)crow.size();
+    crow.push_back((int32_t)kvp.first);
+    for (auto& x : kvp.second) { cslot.push_back(x.first); cval.push_back(x.second); }
+    cptr.push_back((int32_t)cslot.size());
+  }
+  // monitors of slots and correction rows are written by the v5 kernel
+  const int64_t nh = ns + (int64_t)crow.size();
+  std::vector<std::vector<int32_t>> hl(nh);
+  rs.hist_idx.assign(hist_idx, hist_idx + q);
+  for (int64_t k = 0; k < q; ++k) {
+    auto a1 = slot_of.find(hist_idx[k]);
+    auto a2 = cor_of.find(hist_idx[k]);
+    if (a1 != slot_of.end()) { hl[a1->second].push_back((int32_t)k); rs.hist_idx[k] = -1; }
+    else if (a2 != cor_of.end()) { hl[ns + a2->second].push_back((int32_t)k); rs.hist_idx[k] = -1; }
+  }
+  std::vector<int32_t> hp(1, 0), hs;
+  for (auto& l : hl) { hs.insert(hs.end(), l.begin(), l.end()); hp.push_back((int32_t)hs.size()); }
+
+  cudaStream_t st = plan->stream;
+  DevBuf<double> d_sig, d_hist, d_fld, d_dsp, d_accn, d_fout, d_kv, d_cv, d_sm, d_fw, d_cval, d_ud;
+  DevBuf<int32_t> d_er, d_es, d_el, d_sr, d_kp, d_kc, d_cp, d_cc, d_ccs, d_fs, d_crow, d_cptr, d_cslot,
+      d_hp, d_hs;
+  rs.n_sig = p > 0 ? frc_rows : 0;
+  if (rs.n_sig) {
+    std::vector<double> h((size_t)n_t * rs.n_sig);
+    for (int64_t ti = 0; ti < n_t; ++ti)
+      for (int64_t k = 0; k < frc_rows; ++k) h[(size_t)ti * rs.n_sig + k] = frcs[k + frc_rows * ti];
+    CUDA_TRY(d_sig.upload(h));
+    rs.d_sig64 = d_sig.p;
+  }
+  const size_t hist_n = (size_t)q * n_t;
+  CUDA_TRY(d_hist.alloc(hist_n));
+  if (hist_n) CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
+  rs.d_hist = d_hist.p;
+  const int64_t n_frames = every_n > 0 ? (n_t + every_n - 1) / every_n : 0;
+  std::vector<double> ftime(n_frames, 0.0);
+  if (n_frames) {
+    CUDA_TRY(d_fld.alloc((size_t)n * n_frames));
+    CUDA_TRY(cudaMemsetAsync(d_fld.p, 0, (size_t)n * n_frames * sizeof(double), st));
+    rs.every_n = every_n;
+    rs.field_is_vel = 1;
+    rs.d_fld = d_fld.p;
+    rs.fld_time = &ftime;
+  }
+  bfe::V5Args v{};
+  const size_t fout_n = (size_t)r * n_t;
+  if (ns) {
+    CUDA_TRY(d_er.upload(ent_row));
+    CUDA_TRY(d_es.upload(ent_slot));
+    CUDA_TRY(d_el.upload(ent_last));
+    CUDA_TRY(d_dsp.upload(hd));
+    CUDA_TRY(d_accn.upload(ha));
+    CUDA_TRY(d_fout.alloc(fout_n));
+    CUDA_TRY(cudaMemsetAsync(d_fout.p, 0, fout_n * sizeof(double), st));
+    CUDA_TRY(d_sr.upload(slot_row));
+    CUDA_TRY(d_sm.upload(sm));
+    CUDA_TRY(d_kp.upload(kp));
+    CUDA_TRY(d_kc.upload(kc));
+    CUDA_TRY(d_kv.upload(kv));
+    CUDA_TRY(d_cp.upload(cp));
+    CUDA_TRY(d_cc.upload(cc));
+    CUDA_TRY(d_ccs.upload(ccs));
+    CUDA_TRY(d_cv.upload(cv));
+    CUDA_TRY(d_fs.upload(fsig));
+    CUDA_TRY(d_fw.upload(fw));
+    CUDA_TRY(d_crow.upload(crow));
+    CUDA_TRY(d_cptr.upload(cptr));
+    CUDA_TRY(d_cslot.upload(cslot));
+    CUDA_TRY(d_cval.upload(cval));
+    CUDA_TRY(d_hp.upload(hp));
+    CUDA_TRY(d_hs.upload(hs));
+    CUDA_TRY(d_ud.alloc(2 * (size_t)ns));
+    CUDA_TRY(cudaMemsetAsync(d_ud.p, 0, 2 * (size_t)ns * sizeof(double), st));
+    v.n_ent = (int32_t)r;
+    v.ent_row = d_er.p;
+    v.ent_slot = d_es.p;
+    v.ent_last = d_el.p;
+    v.dsp = d_dsp.p;
+    v.accn = d_accn.p;
+    v.frc_out = d_fout.p;
+    v.n_slot = (int32_t)ns;
+    v.slot_row = d_sr.p;
+    v.slot_m = d_sm.p;
+    v.k_ptr = d_kp.p;
+    v.k_col = d_kc.p;
+    v.k_val = d_kv.p;
+    v.c_ptr = d_cp.p;
+    v.c_col = d_cc.p;
+    v.c_cslot = d_ccs.p;
+    v.c_val = d_cv.p;
+    v.f_sig = d_fs.p;
+    v.f_w = d_fw.p;
+    v.n_cor = (int32_t)crow.size();
+    v.cor_row = d_crow.p;
+    v.cor_ptr = d_cptr.p;
+    v.cor_slot = d_cslot.p;
+    v.cor_val = d_cval.p;
+    v.h_ptr = d_hp.p;
+    v.h_slot = d_hs.p;
+    v.dt = dt;
+    rs.v5 = &v;
+    rs.d_ud[0] = d_ud.p;
+    rs.d_ud[1] = d_ud.p + ns;
+  }
+  if ((rc = execute(plan, rs, st))) return rc;
+  if (hist_n) CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (n_frames)
+    CUDA_TRY(cudaMemcpyAsync(fld_out, d_fld.p, (size_t)n * n_frames * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (fout_n) CUDA_TRY(cudaMemcpyAsync(frc_out, d_fout.p, fout_n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (n_frames) std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
   if (dev != plan->device) cudaSetDevice(dev);
   return BFE_OK;
 }

@@ -50,6 +50,11 @@ extern "C" {
 /* solver_mode strings of fn_explicit_dynamic_solver_v6.m:130-139 */
 #define BFE_MODE_VEL_CURRENT 0    /* 'vel at curent time step' (v6.m:135, default) */
 #define BFE_MODE_VEL_LAST_HALF 1  /* 'vel at last half time step' (v6.m:131) */
+/* fn_explicit_dynamic_solver_v5.m:142-188 (acceleration -> velocity ->
+   displacement). Its update equals the 'last half' one; a plan built with this
+   mode also keeps K and C on the host for the prescribed-displacement rows of
+   bfe_run_v5. */
+#define BFE_MODE_V5 2
 
 /* solver_precision of v6.m:57-61,141-159 */
 #define BFE_PREC_DOUBLE 0      /* plain FP64 state and operator */
@@ -126,6 +131,33 @@ int bfe_run(bfe_plan* plan, int64_t n_t, const double* time,
             int64_t q, const int64_t* hist_idx,
             int64_t every_n, int32_t field_is_vel,
             double* hist_out, double* fld_out, double* fld_time_out);
+
+/*
+ * One load step of the v5 scheme, host buffers. Replaces the time loop of
+ * fn_explicit_dynamic_solver_v5.m:60-188 (called from
+ * code/fn_BristolFE_v2.m:115-118 when dynamic_solver_version = 'v5'). The plan
+ * must have been created with BFE_MODE_V5.
+ *   frc_idx[p], frcs         as bfe_run (frc_rows x n_t, frc_rows = 1 or p).
+ *                            v5 keeps the last forcing column when time is
+ *                            longer than forcing_functions (v5.m:145-147):
+ *                            callers pad frcs by repeating it
+ *   dsp_idx[r], dsps         prescribed displacements (v5.m:159-162), dsps is
+ *                            dsp_rows x n_t with dsp_rows = r (or 1 when r = 1);
+ *                            duplicate DOFs take the last row
+ *   hist_idx[q], hist_out    q x n_t displacement histories
+ *   every_n                  field output every n-th sample (<= 0: none);
+ *                            frames hold the velocity (v5.m:168-177)
+ *   frc_out                  r x n_t reaction forces at the prescribed DOFs,
+ *                            m_d accn + K(d,:) u_previous (v5.m:161), accn
+ *                            the second difference of dsps with two leading
+ *                            zero columns (v5.m:73-76); may be NULL when r = 0
+ * The march starts at the first non-zero column of frcs or dsps (v5.m:131-137).
+ */
+int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,
+               int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+               int64_t r, const int64_t* dsp_idx, int64_t dsp_rows, const double* dsps,
+               int64_t q, const int64_t* hist_idx, int64_t every_n,
+               double* hist_out, double* fld_out, double* fld_time_out, double* frc_out);
 
 /*
  * R independent load steps sharing one operator (array full-matrix capture:

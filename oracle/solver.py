@@ -174,6 +174,7 @@ def explicit_dynamic_solver_v5(K, C, M, time, forcing_indices, forcing_functions
         frc_out = np.zeros((disp_idx.size, nt))
         tmp = np.hstack([np.zeros((Dd.shape[0], 2)), Dd])
         accn = (tmp[:, 2:] - 2 * tmp[:, 1:-1] + tmp[:, :-2]) / dt ** 2   # v5.m:73-76
+        same_dof = (disp_idx[:, None] == disp_idx[None, :]).astype(float)
     if np.isinf(field_output_every_n_frames):
         fo_ti = np.zeros(0, np.int64)
         fld, fld_t = None, None
@@ -204,7 +205,10 @@ def explicit_dynamic_solver_v5(K, C, M, time, forcing_indices, forcing_functions
         u = u_prev + dt * ud                                             # v5.m:156
         if disp_idx is not None:                                         # v5.m:159-162
             u[disp_idx] = Dd[:, ti - 1]
-            frc_out[:, ti - 1] = m[disp_idx] * accn[:, ti - 1] + K[disp_idx] @ u_prev
+            # diag_M(d, d) * accn: repeated DOFs in d make diag_M(d, d) a
+            # block of equal masses, so each entry sums the accelerations of
+            # every entry of the same DOF
+            frc_out[:, ti - 1] = m[disp_idx] * (same_dof @ accn[:, ti - 1]) + K[disp_idx] @ u_prev
         if hist is not None:
             hist[:, ti - 1] = u[hist_idx]
         k = frame_of.get(ti)

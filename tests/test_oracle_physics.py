@@ -84,6 +84,24 @@ def test_v5_equals_v6_last_half_step():
     assert np.abs(h5 - h6).max() <= 1e-9 * np.abs(h6).max()
 
 
+def test_v5_prescribing_the_forced_displacement_reproduces_the_run():
+    # v5.m:150-162: prescribing at the forced DOF the displacement history of a
+    # forced run leaves every other DOF's history unchanged (C = 0 there), and
+    # the reaction force m accn + K(d,:) u_previous equals the applied force,
+    # since accn is the scheme's own second difference (v5.m:73-76).
+    m = modelgen.solid_plate(W=2e-3, H=1e-3, h=0.1e-3)
+    nt = 300
+    t, s = modelgen.pulse(nt, m["dt"])
+    fi = modelgen.gi_of(m["gl"], [m["frc_nd"]], 2)
+    hi = np.concatenate([modelgen.gi_of(m["gl"], m["mon_nds"], 2), fi])
+    h1, _, f1, _ = solver.explicit_dynamic_solver_v5(m["K"], m["C"], m["M"], t, fi, s, [], [], hi, np.inf, 0)
+    assert f1 is None
+    ud = h1[-1:]
+    h2, _, f2, _ = solver.explicit_dynamic_solver_v5(m["K"], m["C"], m["M"], t, [], [], fi, ud, hi, np.inf, 0)
+    assert np.abs(h2 - h1).max() <= 1e-12 * np.abs(h1).max()
+    assert np.abs(f2[0] - s).max() <= 1e-9 * np.abs(s).max()
+
+
 def test_undamped_energy_is_bounded():
     m = modelgen.solid_plate(W=2e-3, H=1e-3, h=0.1e-3)
     nt = 400
