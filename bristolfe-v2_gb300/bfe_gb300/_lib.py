@@ -24,6 +24,10 @@ BFE_CSC = 1
 BFE_MODE_VEL_CURRENT = 0
 BFE_MODE_VEL_LAST_HALF = 1
 BFE_MODE_V5 = 2
+BFE_FIELD_SQRT_KE = 0
+BFE_FIELD_MEAN = 1
+BFE_FIELD_DIV = 2
+BFE_FIELD_CURL = 3
 BFE_PREC_DOUBLE = 0
 BFE_PREC_SINGLE = 1
 
@@ -59,6 +63,11 @@ SIGNATURES = {
     "bfe_plan_ndof": (I32, [VP, PI64]),
     "bfe_run": (I32, [VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, I32, PD, PD, PD]),
     "bfe_run_batched": (I32, [VP, I64, I64, PD, I64, PI64, I64, PD, I64, PI64, PD]),
+    "bfe_field_create": (I32, [I32, I32, I64, I64, I32, PD, I32, PI64, I64, I32, PI64, PD,
+                               ctypes.POINTER(VP)]),
+    "bfe_field_destroy": (I32, [VP]),
+    "bfe_field_apply": (I32, [VP, I64, PD, PD]),
+    "bfe_run_field": (I32, [VP, VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, I32, PD, PD, PD]),
     "bfe_run_v5": (I32, [VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, PD, I64, PI64, I64,
                          PD, PD, PD, PD]),
     "bfe_run_device": (I32, [VP, I64, I64, I64, I64, PI64, PI64, PI64, PD, I64, VP,

@@ -170,8 +170,11 @@ class Plan:
         self.close()
 
     def run(self, time, forcing_indices, forcing_functions, history_indices,
-            field_output_every_n_frames=np.inf, field_is_vel=True):
-        """One load step (1-based indices). Returns (hist q x n_t, fld or None, fld_time or None)."""
+            field_output_every_n_frames=np.inf, field_is_vel=True, field=None):
+        """One load step (1-based indices). Returns (hist q x n_t, fld or None, fld_time or None).
+
+        With ``field`` (a FieldOutput of this model) each frame is reduced to
+        element values on the device and fld is n_el x n_frames."""
         time = np.ascontiguousarray(np.asarray(time, float).ravel())
         nt = time.size
         fi = np.ascontiguousarray(np.asarray(forcing_indices, np.int64).ravel() - 1) \
@@ -193,12 +196,16 @@ class Plan:
         fld = fld_t = None
         if every > 0:
             nf = (nt + every - 1) // every
-            fld = np.zeros((self.n, nf), order="F")
+            fld = np.zeros((field.n_el if field is not None else self.n, nf), order="F")
             fld_t = np.zeros(nf)
-        st = self._lib.bfe_run(self._h, nt, ptr(time, ctypes.c_double), p, ptr(fi, ctypes.c_int64),
-                               rows, ptr(F, ctypes.c_double), q, ptr(hi, ctypes.c_int64),
-                               every, int(bool(field_is_vel)), ptr(hist, ctypes.c_double),
-                               ptr(fld, ctypes.c_double), ptr(fld_t, ctypes.c_double))
+        args = (nt, ptr(time, ctypes.c_double), p, ptr(fi, ctypes.c_int64),
+                rows, ptr(F, ctypes.c_double), q, ptr(hi, ctypes.c_int64),
+                every, int(bool(field_is_vel)), ptr(hist, ctypes.c_double),
+                ptr(fld, ctypes.c_double), ptr(fld_t, ctypes.c_double))
+        if field is not None:
+            st = self._lib.bfe_run_field(self._h, field.handle, *args)
+        else:
+            st = self._lib.bfe_run(self._h, *args)
         check(st)
         return hist, fld, fld_t
 

@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+struct bfe_field;
+
 namespace bfe {
 
 // Sliced-ELL slice height: one warp of rows per slice.
@@ -181,6 +183,25 @@ struct V5Args {
   double dt;
 };
 cudaError_t launch_v5(const StepArgs& a, const V5Args& v, int precision, cudaStream_t s);
+
+// Element field output (bfe_field.cu), fn_get_field_output.m:1-135.
+struct FieldArgs {
+  int32_t type;               // BFE_FIELD_*
+  int32_t comp;               // 0-based DOF column (BFE_FIELD_MEAN)
+  int64_t n_el;
+  int32_t el_cols, max_df, dims;
+  const int32_t* els;         // [n_el][el_cols] 0-based node, -1 unused
+  const int32_t* gl;          // [n_nodes][max_df] 0-based global DOF, -1 none
+  const double* m_diag;       // [n] diag(M) (BFE_FIELD_SQRT_KE)
+  const double* uv;           // [n_el][el_cols][dims] unit vectors (div; rotated for curl)
+};
+// out[e] for one frame: the frame is u_new (is_vel = 0) or (u_new - u_old) / dt,
+// u of the plan's precision (0: double, 1: float).
+cudaError_t launch_field(const FieldArgs& f, const void* u_new, const void* u_old, int precision,
+                         int is_vel, double dt, double* out, cudaStream_t s);
+const FieldArgs& field_args(const bfe_field* f);
+int64_t field_ndof(const bfe_field* f);
+int field_device(const bfe_field* f);
 
 // Element data and states of one adjoint gradient contraction (bfe_adjoint.cu).
 struct GradArgs {

@@ -927,6 +927,8 @@ struct RunSpec {
   double* d_fld = nullptr;
   std::vector<double>* fld_time = nullptr;
   const double* time = nullptr;    // host time samples (for frame times)
+  const bfe::FieldArgs* field = nullptr;  // frames reduced to element values (bfe_run_field)
+  double* d_el = nullptr;          // device n_el x n_frames
   const bfe::V5Args* v5 = nullptr; // prescribed-displacement rows (bfe_run_v5)
   double* d_ud[2] = {nullptr, nullptr};
 };
@@ -1147,15 +1149,19 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       stt.aux_launches++;
     }
     double* frame_col = nullptr;
-    if (ti >= 0 && rs.every_n > 0 && rs.d_fld && ti % rs.every_n == 0) {
+    if (ti >= 0 && rs.every_n > 0 && (rs.d_fld || rs.field) && ti % rs.every_n == 0) {
       const int64_t k = ti / rs.every_n;
       if (rec && timing) CUDA_TRY(mark(ev_aux));
-      e = bfe::launch_frame(a, prec, rs.d_fld, k, rs.field_is_vel, pl->dt, st);
+      if (rs.field)
+        e = bfe::launch_field(*rs.field, a.u_new, a.u_n, prec, rs.field_is_vel, pl->dt,
+                              rs.d_el + (size_t)rs.field->n_el * k, st);
+      else
+        e = bfe::launch_frame(a, prec, rs.d_fld, k, rs.field_is_vel, pl->dt, st);
       if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "frame kernel launch failed: %s", cudaGetErrorString(e));
       if (rec && timing) CUDA_TRY(mark(ev_aux));
       stt.aux_launches++;
       if (rs.fld_time) (*rs.fld_time)[k] = rs.time[ti];
-      frame_col = rs.d_fld + (size_t)n * k;
+      if (rs.d_fld) frame_col = rs.d_fld + (size_t)n * k;
     }
     if (rs.v5) {
       bfe::V5Args v = *rs.v5;
@@ -1287,6 +1293,67 @@ int build_forcing(bfe_plan* pl, int64_t R, int64_t p, const int64_t* frc_idx, in
   return BFE_OK;
 }
 
+// One load step with frames (every_n > 0): n x n_frames frames into fld_out,
+// or, with a field, n_el x n_frames element values.
+int run_one(bfe_plan* plan, const bfe_field* field, int64_t n_t, const double* time,
+            int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+            int64_t q, const int64_t* hist_idx, int64_t every_n, int32_t field_is_vel,
+            double* hist_out, double* fld_out, double* fld_time_out) {
+  int rc;
+  if ((rc = check_time(plan, n_t, time))) return rc;
+  if (!fld_out || !fld_time_out) return fail(BFE_ERR_ARG, "fld_out/fld_time_out is NULL");
+  if (q < 0 || p < 0) return fail(BFE_ERR_ARG, "negative sizes");
+  if (q > 0 && (!hist_idx || !hist_out)) return fail(BFE_ERR_ARG, "hist_idx/hist_out is NULL");
+  for (int64_t k = 0; k < q; ++k)
+    if (hist_idx[k] < 0 || hist_idx[k] >= plan->n) return fail(BFE_ERR_ARG, "history index %lld out of range", (long long)hist_idx[k]);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != plan->device) CUDA_TRY(cudaSetDevice(plan->device));
+  RunSpec rs;
+  rs.R = 1;
+  rs.n_t = n_t;
+  rs.time = time;
+  if ((rc = build_forcing(plan, 1, p, frc_idx, frc_rows, rs.frc))) return rc;
+  if (p > 0 && !frcs) return fail(BFE_ERR_ARG, "frcs is NULL");
+  rs.ti_start = p > 0 ? first_nonzero_column(frcs, frc_rows, n_t, 1) : n_t;
+  rs.hist_idx.assign(hist_idx, hist_idx + q);
+  cudaStream_t st = plan->stream;
+  DevBuf<double> d_sig, d_hist, d_fld;
+  rs.n_sig = p > 0 ? frc_rows : 0;
+  if (rs.n_sig) {
+    std::vector<double> h((size_t)n_t * rs.n_sig);
+    for (int64_t ti = 0; ti < n_t; ++ti)
+      for (int64_t k = 0; k < frc_rows; ++k) h[(size_t)ti * rs.n_sig + k] = frcs[k + frc_rows * ti];
+    CUDA_TRY(d_sig.upload(h));
+    rs.d_sig64 = d_sig.p;
+  }
+  const size_t hist_n = (size_t)q * n_t;
+  CUDA_TRY(d_hist.alloc(hist_n));
+  if (hist_n) CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
+  rs.d_hist = d_hist.p;
+  const int64_t n_frames = (n_t + every_n - 1) / every_n;
+  const int64_t rows = field ? bfe::field_args(field).n_el : plan->n;
+  CUDA_TRY(d_fld.alloc((size_t)rows * n_frames));
+  if (rows) CUDA_TRY(cudaMemsetAsync(d_fld.p, 0, (size_t)rows * n_frames * sizeof(double), st));
+  std::vector<double> ftime(n_frames, 0.0);
+  rs.every_n = every_n;
+  rs.field_is_vel = field_is_vel;
+  if (field) {
+    rs.field = &bfe::field_args(field);
+    rs.d_el = d_fld.p;
+  } else {
+    rs.d_fld = d_fld.p;
+  }
+  rs.fld_time = &ftime;
+  if ((rc = execute(plan, rs, st))) return rc;
+  if (hist_n) CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (rows) CUDA_TRY(cudaMemcpyAsync(fld_out, d_fld.p, (size_t)rows * n_frames * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
+  if (dev != plan->device) cudaSetDevice(dev);
+  return BFE_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1349,53 +1416,23 @@ int bfe_run(bfe_plan* plan, int64_t n_t, const double* time,
   if (every_n <= 0) {
     return bfe_run_batched(plan, 1, n_t, time, p, frc_idx, frc_rows, frcs, q, hist_idx, hist_out);
   }
-  int rc;
-  if ((rc = check_time(plan, n_t, time))) return rc;
-  if (!fld_out || !fld_time_out) return fail(BFE_ERR_ARG, "fld_out/fld_time_out is NULL");
-  if (q < 0 || p < 0) return fail(BFE_ERR_ARG, "negative sizes");
-  if (q > 0 && (!hist_idx || !hist_out)) return fail(BFE_ERR_ARG, "hist_idx/hist_out is NULL");
-  for (int64_t k = 0; k < q; ++k)
-    if (hist_idx[k] < 0 || hist_idx[k] >= plan->n) return fail(BFE_ERR_ARG, "history index %lld out of range", (long long)hist_idx[k]);
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev != plan->device) CUDA_TRY(cudaSetDevice(plan->device));
-  RunSpec rs;
-  rs.R = 1;
-  rs.n_t = n_t;
-  rs.time = time;
-  if ((rc = build_forcing(plan, 1, p, frc_idx, frc_rows, rs.frc))) return rc;
-  if (p > 0 && !frcs) return fail(BFE_ERR_ARG, "frcs is NULL");
-  rs.ti_start = p > 0 ? first_nonzero_column(frcs, frc_rows, n_t, 1) : n_t;
-  rs.hist_idx.assign(hist_idx, hist_idx + q);
-  cudaStream_t st = plan->stream;
-  DevBuf<double> d_sig, d_hist, d_fld;
-  rs.n_sig = p > 0 ? frc_rows : 0;
-  if (rs.n_sig) {
-    std::vector<double> h((size_t)n_t * rs.n_sig);
-    for (int64_t ti = 0; ti < n_t; ++ti)
-      for (int64_t k = 0; k < frc_rows; ++k) h[(size_t)ti * rs.n_sig + k] = frcs[k + frc_rows * ti];
-    CUDA_TRY(d_sig.upload(h));
-    rs.d_sig64 = d_sig.p;
+  return run_one(plan, nullptr, n_t, time, p, frc_idx, frc_rows, frcs, q, hist_idx, every_n,
+                 field_is_vel, hist_out, fld_out, fld_time_out);
+}
+
+int bfe_run_field(bfe_plan* plan, const bfe_field* field, int64_t n_t, const double* time,
+                  int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+                  int64_t q, const int64_t* hist_idx, int64_t every_n, int32_t field_is_vel,
+                  double* hist_out, double* el_out, double* fld_time_out) {
+  g_last_error.clear();
+  if (!plan || !field) return fail(BFE_ERR_ARG, "plan or field is NULL");
+  if (bfe::field_ndof(field) != plan->n) return fail(BFE_ERR_ARG, "the field was created for a different number of DOFs");
+  if (bfe::field_device(field) != plan->device) return fail(BFE_ERR_ARG, "the field and the plan are on different devices");
+  if (every_n <= 0) {
+    return bfe_run_batched(plan, 1, n_t, time, p, frc_idx, frc_rows, frcs, q, hist_idx, hist_out);
   }
-  const size_t hist_n = (size_t)q * n_t;
-  CUDA_TRY(d_hist.alloc(hist_n));
-  if (hist_n) CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
-  rs.d_hist = d_hist.p;
-  const int64_t n_frames = (n_t + every_n - 1) / every_n;
-  CUDA_TRY(d_fld.alloc((size_t)plan->n * n_frames));
-  CUDA_TRY(cudaMemsetAsync(d_fld.p, 0, (size_t)plan->n * n_frames * sizeof(double), st));
-  std::vector<double> ftime(n_frames, 0.0);
-  rs.every_n = every_n;
-  rs.field_is_vel = field_is_vel;
-  rs.d_fld = d_fld.p;
-  rs.fld_time = &ftime;
-  if ((rc = execute(plan, rs, st))) return rc;
-  if (hist_n) CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaMemcpyAsync(fld_out, d_fld.p, (size_t)plan->n * n_frames * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaStreamSynchronize(st));
-  std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
-  if (dev != plan->device) cudaSetDevice(dev);
-  return BFE_OK;
+  return run_one(plan, field, n_t, time, p, frc_idx, frc_rows, frcs, q, hist_idx, every_n,
+                 field_is_vel, hist_out, el_out, fld_time_out);
 }
 
 int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,

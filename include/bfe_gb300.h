@@ -160,6 +160,52 @@ int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,
                double* hist_out, double* fld_out, double* fld_time_out, double* frc_out);
 
 /*
+ * Element field values from field frames, on the GPU. Replaces
+ * code/internal/fn_get_field_output.m:1-135 (called from
+ * code/fn_BristolFE_v2.m:145 on every step's frames).
+ */
+#define BFE_FIELD_SQRT_KE 0   /* 'sqrt(KE)', the default for any other string (:64-78) */
+#define BFE_FIELD_MEAN 1      /* 'mean(u<k>)' / 'mean(v<k>)': component = k (1-based) (:35-37) */
+#define BFE_FIELD_DIV 2       /* 'div(u)' / 'div(v)' (:38-58, :85-99) */
+#define BFE_FIELD_CURL 3      /* 'curl(u)' / 'curl(v)', 2D only (:38-58, :101-105) */
+
+typedef struct bfe_field bfe_field;
+
+/*
+ * Mesh maps of one field-output type, uploaded to the current device.
+ *   nds        n_nodes x n_dims node coordinates (column-major; div/curl only,
+ *              may be NULL otherwise)
+ *   gl_lookup  n_nodes x max_df, 1-based global DOF of (node, DOF number),
+ *              0 = none (mats.gl_lookup)
+ *   els        n_el x el_cols, 1-based nodes, 0 = unused column (mod.els)
+ *   m_diag     n values of diag(M) (sqrt(KE) only, may be NULL otherwise)
+ * Element values are means over an element's used nodes; div/curl are the
+ * sums of nodal vectors dotted with the unit vectors from the element centre
+ * to its nodes (zero for elements with an unused column), as the reference.
+ */
+int bfe_field_create(int32_t type, int32_t component, int64_t n,
+                     int64_t n_nodes, int32_t n_dims, const double* nds,
+                     int32_t max_df, const int64_t* gl_lookup,
+                     int64_t n_el, int32_t el_cols, const int64_t* els,
+                     const double* m_diag, bfe_field** out);
+int bfe_field_destroy(bfe_field* field);
+
+/* fld (n x n_frames, host) -> out (n_el x n_frames, host). */
+int bfe_field_apply(bfe_field* field, int64_t n_frames, const double* fld, double* out);
+
+/*
+ * bfe_run with the frames reduced to element values on the device as they
+ * are produced (fn_BristolFE_v2.m:120-147 for one step): el_out is
+ * n_el x n_frames; the n x n_frames frames never leave (or fill) the GPU.
+ * The field must have been created on the plan's device with the plan's n.
+ */
+int bfe_run_field(bfe_plan* plan, const bfe_field* field, int64_t n_t, const double* time,
+                  int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
+                  int64_t q, const int64_t* hist_idx,
+                  int64_t every_n, int32_t field_is_vel,
+                  double* hist_out, double* el_out, double* fld_time_out);
+
+/*
  * R independent load steps sharing one operator (array full-matrix capture:
  * one step per transmitter, subdoms/fn_run_main_model.m:101-115), run as one
  * multi-right-hand-side time march. Host buffers.

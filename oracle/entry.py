@@ -140,8 +140,44 @@ def _average_over_nodes(nv, els):
     return ev.reshape((els.shape[0],) + sz[1:])
 
 
+def element_centres(nds, els):
+    """code/fn_calc_element_centres.m:1-18: mean of each element's nodes."""
+    els = np.asarray(els)
+    c = np.zeros((els.shape[0], nds.shape[1]))
+    n = np.zeros((els.shape[0], 1))
+    for i in range(els.shape[1]):
+        v = els[:, i] > 0
+        j = np.where(v, els[:, i], 1) - 1
+        n += v[:, None]
+        c += nds[j, :] * v[:, None]
+    return c / n
+
+
+def _unit_vecs_div(mod):
+    """fn_get_field_output.m:84-98: unit vectors from each element's centre to
+    its nodes; all zero for elements with an unused node column."""
+    nds, els = mod["nds"], np.asarray(mod["els"])
+    uv = np.zeros(els.shape + (nds.shape[1],))
+    valid = np.ones(els.shape[0], bool)
+    for i in range(els.shape[1]):
+        valid &= els[:, i] > 0
+        j = np.where(els[:, i] > 0, els[:, i], 1) - 1
+        uv[:, i, :] = nds[j, :]
+    uv = uv - element_centres(nds, els)[:, None, :]
+    uv = uv / np.sqrt((uv ** 2).sum(axis=2, keepdims=True))
+    uv[~valid] = 0.0
+    return uv
+
+
+def _unit_vecs_curl(mod):
+    """fn_get_field_output.m:100-104: div vectors rotated by 90 degrees."""
+    uv = _unit_vecs_div(mod)
+    return np.stack([uv[:, :, 1], -uv[:, :, 0]], axis=2)
+
+
 def get_field_output(f_out, mod, mats, field_output_type="sqrt(KE)"):
-    """fn_get_field_output.m:1-107 ('KE' default, mean(ui)/mean(vi), raw)."""
+    """fn_get_field_output.m:1-80 ('sqrt(KE)' default, mean(ui)/mean(vi),
+    div/curl, raw)."""
     t = field_output_type
     if t in ("mean(u1)", "mean(u2)", "mean(u3)", "mean(v1)", "mean(v2)", "mean(v3)"):
         nv = _global_to_nodal(f_out, mats["gl_lookup"])
@@ -150,7 +186,20 @@ def get_field_output(f_out, mod, mats, field_output_type="sqrt(KE)"):
     if t in ("raw(u)", "raw(v)"):
         return t
     if t in ("curl(u)", "div(u)", "curl(v)", "div(v)"):
-        raise NotImplementedError("div/curl field output is not part of the oracle")
+        nv = _global_to_nodal(f_out, mats["gl_lookup"])                 # :34
+        if t.startswith("div"):
+            uv = _unit_vecs_div(mod)                                    # :49-50
+        else:
+            if mod["nds"].shape[1] > 2:                                 # :52-54
+                raise ValueError("Cannot output curl for 3D models")
+            uv = _unit_vecs_curl(mod)
+        els = np.asarray(mod["els"])
+        v = np.zeros((els.shape[0], f_out.shape[1]))                    # :58-63
+        d = uv.shape[2]
+        for i in range(els.shape[1]):
+            j = np.where(els[:, i] > 0, els[:, i], 1) - 1
+            v = v + (nv[j, :, :d] * uv[:, i, None, :]).sum(axis=2)
+        return v
     dM = mats["M"].diagonal()
     KE_g = np.abs(f_out ** 2 * dM[:, None]) / 2                       # :64-67
     KE_n = _global_to_nodal(KE_g, mats["gl_lookup"]).sum(axis=2)        # :70-71
