@@ -146,7 +146,9 @@ KERNEL_NAMES = {
     6: "step_f32_group<2>", 7: "step_f32_group<4>", 8: "step_f32_group_async",
     9: "step_f32_group2<2,1,1>", 10: "step_f32_group2<2,2,1>", 11: "step_f32_group2<2,4,1>",
     12: "step_f32_group2<2,1,4>", 13: "step_f32_group2<2,1,6>", 14: "step_f32_group2<2,1,8>",
-    15: "step_f32_group_tma",
+    15: "step_f32_group_tma", 16: "step_f32_group4<1,10>", 17: "step_f32_group4<2,8>",
+    18: "step_f32_group4<1,12>", 19: "step_f32_group4<1,12,late>", 20: "step_f32_group4<1,12,raw>",
+    21: "step_f32_group4<1,12,late,raw>", 22: "step_f32_group4<1,10,raw>",
 }
 
 
@@ -159,7 +161,7 @@ def profiled_traffic(kernel, n_dof):
             d = json.load(f)
     except (OSError, ValueError):
         return None
-    rec = d.get(kernel)
+    rec = d.get(kernel) or d.get(d.get("_same_traffic", {}).get(kernel, ""))
     if not rec:
         return None
     return rec["dram_bytes_per_launch"] * n_dof / rec["n_dof"]

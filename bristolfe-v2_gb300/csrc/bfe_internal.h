@@ -112,6 +112,7 @@ struct GroupArgs {
   const float* coef[kMaxGroups];     // BS*BS per neighbour block, [own k][neighbour l]
   const int32_t* frow[kMaxGroups];   // flat neighbour rows: BS rows per neighbour block
   const float2* coef2[kMaxGroups];   // the coefficients as broadcast pairs {c, c}
+  const int4* rec[kMaxGroups];       // per node {first row, first neighbour block, neighbour count, 0}
 };
 
 // Extra data of the TMA-staged group kernel (bfe_tma.cu): per node the

@@ -849,6 +849,137 @@ __global__ void __launch_bounds__(256, MINB) step_f32_group2(StepArgs a, GroupAr
   else group2_node<MAXBS, UNROLL>(a, gr, gi, node, lane);
 }
 
+// Group block-sparse kernel with a half-warp per node: each lane carries four
+// right-hand sides (float4), so every load, address and index instruction
+// serves two nodes, and a warp holds two nodes' work at the cost of one.
+// UNROLL neighbours are loaded before they are used; LATE_UP reads u_{n-1}
+// only in the epilogue (fewer live registers); RAW reads a 2 x 2 block's
+// coefficients with one 16-byte load of the plain [k][l] array and forms the
+// broadcast pairs in registers (half the coefficient bytes and loads).
+__device__ __forceinline__ float4 f4sub(float4 a, float4 b) {
+  const float2 lo = f2sub(make_float2(a.x, a.y), make_float2(b.x, b.y));
+  const float2 hi = f2sub(make_float2(a.z, a.w), make_float2(b.z, b.w));
+  return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+__device__ __forceinline__ float4 f4fma(float2 c, float4 x, float4 acc) {   // c.x == c.y
+  const float2 lo = __ffma2_rn(c, make_float2(x.x, x.y), make_float2(acc.x, acc.y));
+  const float2 hi = __ffma2_rn(c, make_float2(x.z, x.w), make_float2(acc.z, acc.w));
+  return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+// One neighbour block of a node: acc_k += sum_l c_kl (u_own_l - u_nbr_l).
+template <int BS, bool RAW>
+__device__ __forceinline__ void group4_nbr(const float* nb, const float2* coef, const float* craw, int e,
+                                           size_t rs, const float4 (&uo)[BS], float4 (&acc)[BS]) {
+  float4 g[BS];
+#pragma unroll
+  for (int l = 0; l < BS; ++l) g[l] = __ldg(reinterpret_cast<const float4*>(nb + l * rs));
+  float2 cv[BS * BS];
+  if (RAW && BS == 2) {
+    const float4 cr = __ldg(reinterpret_cast<const float4*>(craw + (size_t)e * 4));
+    cv[0] = make_float2(cr.x, cr.x);
+    cv[1] = make_float2(cr.y, cr.y);
+    cv[2 % (BS * BS)] = make_float2(cr.z, cr.z);
+    cv[3 % (BS * BS)] = make_float2(cr.w, cr.w);
+  } else if (RAW) {
+    const float cr = __ldg(craw + e);
+    cv[0] = make_float2(cr, cr);
+  } else if (BS == 2) {
+    const float4 c0 = __ldg(reinterpret_cast<const float4*>(coef + (size_t)e * 4));
+    const float4 c1 = __ldg(reinterpret_cast<const float4*>(coef + (size_t)e * 4 + 2));
+    cv[0] = make_float2(c0.x, c0.y);
+    cv[1] = make_float2(c0.z, c0.w);
+    cv[2 % (BS * BS)] = make_float2(c1.x, c1.y);
+    cv[3 % (BS * BS)] = make_float2(c1.z, c1.w);
+  } else {
+    cv[0] = __ldg(coef + e);
+  }
+#pragma unroll
+  for (int l = 0; l < BS; ++l) {
+    const float4 dn = f4sub(uo[l], g[l]);                     // u_own - u_nbr
+#pragma unroll
+    for (int k = 0; k < BS; ++k) acc[k] = f4fma(cv[k * BS + l], dn, acc[k]);
+  }
+}
+
+template <int BS, int UNROLL, bool LATE_UP, bool RAW>
+__device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& gr, int gi, int node,
+                                            int l16) {
+  const int4 rec = __ldg(gr.rec[gi] + node);
+  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
+  const int R = a.R;
+  const size_t rs = (size_t)R;
+  const float* un = static_cast<const float*>(a.u_n);
+  const int32_t* nrow = gr.nrow[gi];
+  const float2* coef = gr.coef2[gi];
+  const float* craw = gr.coef[gi];
+  for (int c = l16 * 4; c < R; c += 64) {
+    float4 uo[BS], up[BS], acc[BS];
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      uo[k] = __ldg(reinterpret_cast<const float4*>(un + (size_t)(row0 + k) * rs + c));
+      if (!LATE_UP)
+        up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) +
+                                                        (size_t)(row0 + k) * rs + c));
+      acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll UNROLL
+    for (int e = p0; e < p1; ++e)
+      group4_nbr<BS, RAW>(un + (size_t)__ldg(nrow + e) * rs + c, coef, craw, e, rs, uo, acc);
+    float* unew = static_cast<float*>(a.u_new);
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      const int row = row0 + k;
+      const uint32_t info = __ldg(a.rowinfo + row);
+      const float q = __ldg(static_cast<const float*>(a.rowc) + row);
+      const size_t o = (size_t)row * rs + c;
+      if (LATE_UP) up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) + o));
+      const float2 q2 = make_float2(q, q);
+      float2 res[2], vin[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float2 u = h ? make_float2(uo[k].z, uo[k].w) : make_float2(uo[k].x, uo[k].y);
+        const float2 p = h ? make_float2(up[k].z, up[k].w) : make_float2(up[k].x, up[k].y);
+        const float2 ac = h ? make_float2(acc[k].z, acc[k].w) : make_float2(acc[k].x, acc[k].y);
+        float2 d, err;
+        two_sum2(u, make_float2(-p.x, -p.y), d, err);
+        float2 inc = __ffma2_rn(q2, d, ac);                    // q d - Lp u
+        if (info & kRowForced)
+          inc = __fadd2_rn(inc, make_float2(forcing_sum<float>(a, row, c + 2 * h),
+                                            forcing_sum<float>(a, row, c + 2 * h + 1)));
+        inc = __ffma2_rn(q2, err, inc);
+        res[h] = __fadd2_rn(u, inc);
+        vin[h] = a.int_base_prev ? __fadd2_rn(__fadd2_rn(d, err), inc) : __fadd2_rn(d, err);
+      }
+      *reinterpret_cast<float4*>(unew + o) = make_float4(res[0].x, res[0].y, res[1].x, res[1].y);
+      if (info & kRowInterface) {
+        const int t = lower_bound_i32(a.int_row, a.n_int, row);
+        *reinterpret_cast<float4*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) =
+            make_float4(vin[0].x, vin[0].y, vin[1].x, vin[1].y);
+      } else if (info & kRowMonitored) {
+        write_history(a, row, c, (double)res[0].x);
+        write_history(a, row, c + 1, (double)res[0].y);
+        write_history(a, row, c + 2, (double)res[1].x);
+        write_history(a, row, c + 3, (double)res[1].y);
+      }
+    }
+  }
+}
+
+// 128 threads = 8 half-warps = the 8 nodes of one CTA of the group layout.
+template <int UNROLL, int MINB, bool LATE_UP, bool RAW>
+__global__ void __launch_bounds__(128, MINB) step_f32_group4(StepArgs a, GroupArgs gr) {
+  const int b = blockIdx.x;
+  int gi = 0;
+#pragma unroll
+  for (int k = 1; k < kMaxGroups; ++k)
+    if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
+  const int node = (b - gr.blk_begin[gi]) * 8 + (threadIdx.x >> 4);
+  if (node >= gr.n_nodes[gi]) return;
+  if (gr.bs[gi] == 1) group4_node<1, UNROLL * 2, LATE_UP, RAW>(a, gr, gi, node, threadIdx.x & 15);
+  else group4_node<2, UNROLL, LATE_UP, RAW>(a, gr, gi, node, threadIdx.x & 15);
+}
+
 // ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
@@ -993,8 +1124,13 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 // 9, 10, 11 = packed-math group kernel (unroll 1, 2, 4), 12-14 = the same
 // with occupancy hints of 4, 6 and 8 resident CTAs.
 // 15 = TMA-staged group kernel (bfe_tma.cu; launched by the plan code).
+// 16-22 = half-warp-per-node float4 group kernel: 16 unroll 1 at occupancy
+// hint 10 CTAs of 128 threads, 17 unroll 2 at 8, 18 unroll 1 at 12, 19 the
+// same with u_{n-1} read in the epilogue, 20-22 with one 16-byte load of each
+// block's coefficients (hint 12, 12 with the late u_{n-1}, 10); block sizes
+// <= 2 (3D plans fall back to variant 14).
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
-  if (precision == 1 && R % 64 == 0) return have_groups ? 16 : (have_nodes ? 6 : 4);
+  if (precision == 1 && R % 64 == 0) return have_groups ? 23 : (have_nodes ? 6 : 4);
   return 1;
 }
 
@@ -1018,11 +1154,25 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
-  } else if (a.R % 64 == 0 && variant >= 9 && variant <= 14 && gr) {
+  } else if (a.R % 64 == 0 && variant >= 9 && variant <= 22 && gr) {
     int maxbs = 1;
     for (int k = 0; k < gr->n_groups; ++k) maxbs = gr->bs[k] > maxbs ? gr->bs[k] : maxbs;
-    if (maxbs <= 2) launch_group2<2>(a, *gr, variant, st);
-    else launch_group2<3>(a, *gr, variant, st);
+    const int grid = gr->blk_begin[gr->n_groups];
+    if (variant >= 16 && maxbs <= 2) {
+      switch (variant) {
+        case 16: step_f32_group4<1, 10, false, false><<<grid, 128, 0, st>>>(a, *gr); break;
+        case 17: step_f32_group4<2, 8, false, false><<<grid, 128, 0, st>>>(a, *gr); break;
+        case 18: step_f32_group4<1, 12, false, false><<<grid, 128, 0, st>>>(a, *gr); break;
+        case 19: step_f32_group4<1, 12, true, false><<<grid, 128, 0, st>>>(a, *gr); break;
+        case 20: step_f32_group4<1, 12, false, true><<<grid, 128, 0, st>>>(a, *gr); break;
+        case 21: step_f32_group4<1, 12, true, true><<<grid, 128, 0, st>>>(a, *gr); break;
+        default: step_f32_group4<1, 10, false, true><<<grid, 128, 0, st>>>(a, *gr); break;
+      }
+    } else if (maxbs <= 2) {
+      launch_group2<2>(a, *gr, variant >= 16 ? 14 : variant, st);
+    } else {
+      launch_group2<3>(a, *gr, variant >= 16 ? 14 : variant, st);
+    }
   } else if (a.R % 64 == 0 && variant == 8 && gr) {
     static int sm_count = 0;
     if (sm_count == 0) {

@@ -262,6 +262,7 @@ struct bfe_plan {
   DevBuf<int32_t> g_row0[bfe::kMaxGroups], g_nptr[bfe::kMaxGroups], g_nrow[bfe::kMaxGroups];
   DevBuf<int32_t> g_frow[bfe::kMaxGroups];
   DevBuf<float2> g_coef2[bfe::kMaxGroups];
+  DevBuf<int4> g_rec[bfe::kMaxGroups];
   DevBuf<int32_t> g_cofs[bfe::kMaxGroups];
   DevBuf<float2> g_coefp[bfe::kMaxGroups];
   DevBuf<int> d_err;
@@ -734,6 +735,11 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         for (size_t k = 0; k < coef.size(); ++k) coef2[k] = make_float2(coef[k], coef[k]);
         CUDA_TRY(pl->g_coef2[gi].upload(coef2));
         pl->groups.coef2[gi] = pl->g_coef2[gi].p;
+        std::vector<int4> rec(row0s[gi].size());
+        for (size_t a0 = 0; a0 < rec.size(); ++a0)
+          rec[a0] = make_int4(row0s[gi][a0], nptr[a0], nptr[a0 + 1] - nptr[a0], 0);
+        CUDA_TRY(pl->g_rec[gi].upload(rec));
+        pl->groups.rec[gi] = pl->g_rec[gi].p;
         // padded copy: each node's pairs start on a 16-byte boundary
         std::vector<int32_t> cofs;
         std::vector<float2> coefp;

@@ -173,12 +173,13 @@ def test_errors_through_the_abi(bfe, plate):
             plan.run(t, [1, 2], np.ones((3, 20)), [1])             # 3 rows for 2 DOFs
 
 
-@pytest.mark.parametrize("variant", list(range(16)))
+@pytest.mark.parametrize("variant", list(range(23)))
 def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
     """Each kernel the autotuner can pick (forced through BFE_VARIANT) gives
     the same answers; variants 4, 5 are the node-block kernel, 6, 7 the
     group block-sparse kernel, 8 its cp.async-staged form and 9-14 its
-    packed FP32x2 form and 15 the TMA-staged form."""
+    packed FP32x2 form, 15 the TMA-staged form and 16-22 the half-warp
+    float4 form."""
     m = coupled
     nt = 150
     t, s = modelgen.pulse(nt, m["dt"])
