@@ -24,6 +24,9 @@ BFE_CSC = 1
 BFE_MODE_VEL_CURRENT = 0
 BFE_MODE_VEL_LAST_HALF = 1
 BFE_MODE_V5 = 2
+BFE_EL_CPE3 = 0
+BFE_EL_AC2D3 = 1
+BFE_EL_ASI2D2 = 2
 BFE_FIELD_SQRT_KE = 0
 BFE_FIELD_MEAN = 1
 BFE_FIELD_DIV = 2
@@ -42,6 +45,20 @@ VP = ctypes.c_void_p
 class BfeSparse(ctypes.Structure):
     _fields_ = [("n_rows", I64), ("n_cols", I64), ("nnz", I64), ("format", I32),
                 ("ptr", PI64), ("idx", PI64), ("val", PD)]
+
+
+class BfeMesh2d(ctypes.Structure):
+    _fields_ = [("n_nodes", I64), ("nds", PD), ("n_el", I64), ("el_cols", I32), ("els", PI64),
+                ("el_mat", PI32), ("el_abs", PD), ("el_typ", PI32)]
+
+
+class BfeMaterial(ctypes.Structure):
+    _fields_ = [("el_typ", I32), ("rho", ctypes.c_double), ("D", ctypes.c_double * 36)]
+
+
+class BfeAssemblyOptions(ctypes.Structure):
+    _fields_ = [("dof_mask", I32), ("damping_power_law", ctypes.c_double),
+                ("max_damping", ctypes.c_double), ("max_stiffness_reduction", ctypes.c_double)]
 
 
 class BfeStats(ctypes.Structure):
@@ -63,6 +80,13 @@ SIGNATURES = {
     "bfe_plan_ndof": (I32, [VP, PI64]),
     "bfe_run": (I32, [VP, I64, PD, I64, PI64, I64, PD, I64, PI64, I64, I32, PD, PD, PD]),
     "bfe_run_batched": (I32, [VP, I64, I64, PD, I64, PI64, I64, PD, I64, PI64, PD]),
+    "bfe_assemble_2d": (I32, [ctypes.POINTER(BfeMesh2d), I32, ctypes.POINTER(BfeMaterial),
+                              ctypes.POINTER(BfeAssemblyOptions), ctypes.POINTER(VP)]),
+    "bfe_matrices_info": (I32, [VP, PI64, PI64, PI64, PI64, PI64, PI32]),
+    "bfe_matrices_copy": (I32, [VP, I32, PI64, PI64, PD]),
+    "bfe_matrices_gl_lookup": (I32, [VP, PI64]),
+    "bfe_matrices_destroy": (I32, [VP]),
+    "bfe_plan_create_assembled": (I32, [VP, ctypes.c_double, I32, I32, ctypes.POINTER(VP)]),
     "bfe_field_create": (I32, [I32, I32, I64, I64, I32, PD, I32, PI64, I64, I32, PI64, PD,
                                ctypes.POINTER(VP)]),
     "bfe_field_destroy": (I32, [VP]),

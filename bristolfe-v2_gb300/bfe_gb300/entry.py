@@ -34,6 +34,7 @@ DEFAULT_RUN_OPTIONS = dict(                  # fn_FE_entry_point.m:23-35, fn_bui
     field_output_every_n_frames=np.inf,
     dof_to_use=[],
     batch_steps=True,
+    assemble_on_gpu=True,
 )
 
 
@@ -86,11 +87,21 @@ def add_interface_damping(els, el_typ_i, K, C, M, gl_lookup, factor):
 
 def build_matrices(mod, matls, opt):
     """fn_build_global_matrices_v5 for the 2D element types (CPE3, AC2D3,
-    ASI2D2): K, C, M and gl_lookup."""
+    ASI2D2): K, C, M and gl_lookup, assembled on the GPU (``assemble_on_gpu``,
+    the default) or by the vectorised host builder."""
     typ_names = list(mod["el_typ_i"])
     unknown = sorted(set(typ_names) - set(model.TYPE_CODES))
     if unknown:
         raise SolverError("element types %s are not supported by the GPU path's builder" % unknown)
+    if opt.get("assemble_on_gpu", True):
+        from .assembly import assemble_gpu
+        K, C, M, gl = assemble_gpu(mod["nds"], mod["els"], mod["el_mat_i"], mod["el_abs_i"], typ_names, matls,
+                                   dof_to_use=opt["dof_to_use"], damping_power_law=opt["damping_power_law"],
+                                   max_damping=opt["max_damping"],
+                                   max_stiffness_reduction=opt["max_stiffness_reduction"])
+        if opt["interface_damping_factor"]:
+            C = add_interface_damping(mod["els"], typ_names, K, C, M, gl, opt["interface_damping_factor"])
+        return K, C, M, gl
     typ = np.array([model.TYPE_CODES[t] for t in typ_names])
     K, C, M, gl = model.assemble(np.asarray(mod["nds"], float), np.asarray(mod["els"], np.int64),
                                  np.asarray(mod["el_mat_i"], np.int64).ravel(),

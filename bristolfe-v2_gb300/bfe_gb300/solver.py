@@ -142,6 +142,24 @@ class Plan:
         self.n = nn.value
         return self, offs
 
+    @classmethod
+    def from_handle_factory(cls, create, n, dt, solver_mode=VEL_CURRENT, solver_precision="double"):
+        """A Plan whose handle comes from create(out, mode_code, precision_code)
+        (e.g. bfe_plan_create_assembled)."""
+        lib = _lib.load()
+        self = cls.__new__(cls)
+        self._lib = lib
+        self.mode = _mode_code(solver_mode)
+        self.precision = _precision_code(solver_precision)
+        self.dt = float(dt)
+        handle = ctypes.c_void_p()
+        check(create(ctypes.byref(handle), self.mode, self.precision))
+        self._h = handle
+        nn = ctypes.c_int64()
+        check(lib.bfe_plan_ndof(self._h, ctypes.byref(nn)))
+        self.n = nn.value
+        return self
+
     def set_timing(self, enable=True):
         """CUDA-event timing of every launch in later runs (see stats())."""
         check(self._lib.bfe_plan_set_timing(self._h, int(bool(enable))))

@@ -811,6 +811,36 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   return BFE_OK;
 }
 
+int bfe_plan_create_assembled(const bfe_matrices* mats, double dt, int32_t solver_mode, int32_t precision,
+                              bfe_plan** out) {
+  g_last_error.clear();
+  if (!mats || !out) return fail(BFE_ERR_ARG, "NULL argument");
+  int64_t n = 0, nnz[3] = {0, 0, 0}, n_nodes = 0;
+  int32_t max_df = 0;
+  int rc = bfe_matrices_info(mats, &n, &nnz[0], &nnz[1], &nnz[2], &n_nodes, &max_df);
+  if (rc) return rc;
+  std::vector<int64_t> ptr[3], idx[3];
+  std::vector<double> val[3];
+  bfe_sparse v[3];
+  for (int x = 0; x < 3; ++x) {
+    ptr[x].resize(n + 1);
+    idx[x].resize(std::max<int64_t>(nnz[x], 1));
+    val[x].resize(std::max<int64_t>(nnz[x], 1));
+    if ((rc = bfe_matrices_copy(mats, x, ptr[x].data(), idx[x].data(), val[x].data()))) return rc;
+    v[x] = bfe_sparse{n, n, nnz[x], BFE_CSR, ptr[x].data(), idx[x].data(), val[x].data()};
+  }
+  std::vector<int64_t> gl((size_t)n_nodes * max_df);
+  if ((rc = bfe_matrices_gl_lookup(mats, gl.data()))) return rc;
+  std::vector<int64_t> dof_node(n, -1);
+  std::vector<int32_t> dof_type(n, 0);
+  for (int32_t d = 0; d < max_df; ++d)
+    for (int64_t a = 0; a < n_nodes; ++a) {
+      const int64_t g = gl[a + n_nodes * d];
+      if (g > 0) { dof_node[g - 1] = a; dof_type[g - 1] = d + 1; }
+    }
+  return bfe_plan_create(&v[0], &v[1], &v[2], dt, solver_mode, precision, dof_node.data(), dof_type.data(), out);
+}
+
 int bfe_plan_create_multi(int32_t n_models, const bfe_sparse* K, const bfe_sparse* C,
                           const bfe_sparse* M, double dt, int32_t solver_mode, int32_t precision,
                           const int64_t* const* dof_node, const int32_t* const* dof_type,

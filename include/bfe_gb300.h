@@ -206,6 +206,60 @@ int bfe_run_field(bfe_plan* plan, const bfe_field* field, int64_t n_t, const dou
                   double* hist_out, double* el_out, double* fld_time_out);
 
 /*
+ * Global assembly of a 2D model on the GPU. Replaces the MATLAB-side builder
+ * code/internal/fn_build_global_matrices_v5.m:66-164 (element routines
+ * fn_el_CPE3.m, fn_el_AC2D3.m, fn_el_ASI2D2.m, absorbing grading :115-116,
+ * duplicate summation :145-147, DOF reduction fn_reduce_global_matrices.m,
+ * lookup fn_create_fast_lookup.m). Global DOF numbering is the reference's:
+ * node-major over max_df = the largest DOF number in use, then compacted to
+ * the DOFs whose column has a non-zero in K, C or M. The interface damping of
+ * fn_add_interface_damping.m is not applied here.
+ */
+#define BFE_EL_CPE3 0      /* 3-node plane-strain triangle, DOFs 1-3 */
+#define BFE_EL_AC2D3 1     /* 3-node acoustic triangle, DOF 4 */
+#define BFE_EL_ASI2D2 2    /* 2-node fluid-solid interface, DOFs 1-4 */
+
+typedef struct bfe_mesh2d {
+  int64_t n_nodes;
+  const double* nds;       /* n_nodes x 2, column-major (mod.nds) */
+  int64_t n_el;
+  int32_t el_cols;
+  const int64_t* els;      /* n_el x el_cols, 1-based nodes, 0 = unused (mod.els) */
+  const int32_t* el_mat;   /* 1-based material index (mod.el_mat_i); 0 allowed for ASI2D2 */
+  const double* el_abs;    /* absorbing index in [0, 1] (mod.el_abs_i); NULL = 0 */
+  const int32_t* el_typ;   /* BFE_EL_* (mod.el_typ_i) */
+} bfe_mesh2d;
+
+typedef struct bfe_material {
+  int32_t el_typ;          /* BFE_EL_* the material is meant for (informative) */
+  double rho;              /* density */
+  double D[36];            /* 6 x 6 stiffness, column-major (CPE3); D[0] = bulk modulus (AC2D3) */
+} bfe_material;
+
+typedef struct bfe_assembly_options {
+  int32_t dof_mask;                 /* bit d-1 set: DOF d kept (fe_options.dof_to_use); 0 = all */
+  double damping_power_law;         /* 3 in the reference */
+  double max_damping;               /* 3.1415e7 */
+  double max_stiffness_reduction;   /* 0.01 */
+} bfe_assembly_options;
+
+typedef struct bfe_matrices bfe_matrices;
+
+/* opt may be NULL (the reference's defaults). The matrices stay on the device. */
+int bfe_assemble_2d(const bfe_mesh2d* mesh, int32_t n_mat, const bfe_material* matls,
+                    const bfe_assembly_options* opt, bfe_matrices** out);
+int bfe_matrices_info(const bfe_matrices* m, int64_t* n_dof, int64_t* nnz_k, int64_t* nnz_c,
+                      int64_t* nnz_m, int64_t* n_nodes, int32_t* max_df);
+/* CSR of K (which = 0), C (1) or M (2): ptr has n_dof + 1 entries. */
+int bfe_matrices_copy(const bfe_matrices* m, int32_t which, int64_t* ptr, int64_t* idx, double* val);
+/* gl_lookup: n_nodes x max_df, column-major, 1-based global DOF or 0 (mats.gl_lookup). */
+int bfe_matrices_gl_lookup(const bfe_matrices* m, int64_t* gl_lookup);
+int bfe_matrices_destroy(bfe_matrices* m);
+/* bfe_plan_create on assembled matrices (node/DOF maps from their lookup). */
+int bfe_plan_create_assembled(const bfe_matrices* m, double dt, int32_t solver_mode, int32_t precision,
+                              bfe_plan** out);
+
+/*
  * R independent load steps sharing one operator (array full-matrix capture:
  * one step per transmitter, subdoms/fn_run_main_model.m:101-115), run as one
  * multi-right-hand-side time march. Host buffers.

@@ -128,3 +128,20 @@ def test_dof_maps_from_lookup():
     node, typ = S.dof_maps_from_lookup(gl, 6)
     assert node.tolist() == [0, 0, 1, 1, 1, 2]
     assert typ.tolist() == [1, 2, 1, 2, 4, 4]
+
+
+def test_assembly_argument_errors_are_caught_on_host():
+    """bfe_assemble_2d validates the mesh before touching a device."""
+    import bfe_gb300
+    import modelgen
+    m = modelgen.solid_plate(W=1e-3, H=1e-3, h=0.2e-3)
+    mod = m["mod"]
+    els = np.array(mod["els"]).copy()
+    els[3, 1] = mod["nds"].shape[0] + 7
+    with pytest.raises(bfe_gb300.BfeError, match="node out of range"):
+        bfe_gb300.assemble_gpu(mod["nds"], els, mod["el_mat_i"], None, m["typ"], m["matls"])
+    with pytest.raises(bfe_gb300.BfeError, match="material out of range"):
+        bfe_gb300.assemble_gpu(mod["nds"], mod["els"], np.full(len(els), 5), None, m["typ"], m["matls"])
+    bad = np.array(m["typ"], dtype=object)
+    with pytest.raises(KeyError):
+        bfe_gb300.assemble_gpu(mod["nds"], mod["els"], mod["el_mat_i"], None, ["HEX8"] * len(bad), m["matls"])

@@ -30,7 +30,8 @@ def test_index_mapping_matches_oracle():
 def test_builder_with_interface_damping_matches_oracle():
     from bfe_gb300.entry import DEFAULT_RUN_OPTIONS, build_matrices
     m = modelgen.coupled_model(W=2e-3, Hw=1e-3, Hs=1e-3, h=0.1e-3, abs_thick=0.3e-3)
-    opt = dict(DEFAULT_RUN_OPTIONS, dof_to_use=[1, 2, 4], damping_power_law=2, interface_damping_factor=0.5)
+    opt = dict(DEFAULT_RUN_OPTIONS, dof_to_use=[1, 2, 4], damping_power_law=2, interface_damping_factor=0.5,
+               assemble_on_gpu=False)
     K, C, M, gl = build_matrices(m["mod"], m["matls"], opt)
     Ko, Co, Mo, glo = oassembly.build_global_matrices_v5(m["mod"]["nds"], m["mod"]["els"], m["mod"]["el_mat_i"],
                                                          m["mod"]["el_abs_i"], m["mod"]["el_typ_i"], m["matls"],
