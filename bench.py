@@ -366,6 +366,7 @@ def run_ours(args):
 
     extra = {}
     if rank == 0 and not args.no_extra:
+        extra["fmc_c2a"] = fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, mon_parts[0].size, sig, stream)
         extra["assembly_c1"] = assembly_section(torch, bfe_gb300, model, main)
         extra["hex3d_c3"] = hex3d_section(torch, bfe_gb300, model)
         extra["adjoint_c4"] = adjoint_section(torch, bfe_gb300, model)
@@ -415,6 +416,38 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+def fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, n_rx, sig, stream):
+    """Full-matrix capture of the coupled model's array from the headline
+    march's device history: 64 x 64 transmitter/receiver pairs gathered and
+    convolved with the toneburst on the GPU (fn_parse_to_fmc), checked on 16
+    pairs against the FFT convolution of fn_convolve on the host."""
+    from bfe_gb300.fmc import fmc_from_device_history
+    tx = [a for a in range(R) for _ in range(n_rx)]
+    rx_slots = [[b] for _ in range(R) for b in range(n_rx)]
+    rx_w = [[1.0]] * len(tx)
+    d_out = torch.zeros((len(tx), n_t), dtype=torch.float64, device="cuda")
+    fmc_from_device_history(d_hist, q, n_t, R, tx, rx_slots, rx_w, sig, d_out, stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fmc_from_device_history(d_hist, q, n_t, R, tx, rx_slots, rx_w, sig, d_out, stream.cuda_stream)
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    out = d_out.cpu().numpy()
+    hist = d_hist.cpu().numpy()
+    rng = np.random.default_rng(5)
+    picks = rng.choice(len(tx), 16, replace=False)
+    t0 = time.perf_counter()
+    errs = []
+    for k in picks:
+        trace = hist[tx[k], :, rx_slots[k][0]]
+        F = np.fft.fft(trace, 2 * n_t) * np.fft.fft(sig, 2 * n_t)
+        ref = np.fft.ifft(F).real[:n_t]
+        errs.append(float(np.abs(out[k] - ref).max() / max(np.abs(ref).max(), 1e-300)))
+    host_per_pair = (time.perf_counter() - t0) / len(picks)
+    return {"pairs": len(tx), "samples": n_t, "gpu_s": gpu_s, "host_fft_s_per_pair": host_per_pair,
+            "host_fft_s_all_pairs_estimate": host_per_pair * len(tx), "max_rel_err_vs_fft_16_pairs": max(errs)}
 
 
 def assembly_section(torch, bfe_gb300, model, m):

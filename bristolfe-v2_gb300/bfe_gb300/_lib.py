@@ -87,6 +87,12 @@ SIGNATURES = {
     "bfe_matrices_gl_lookup": (I32, [VP, PI64]),
     "bfe_matrices_destroy": (I32, [VP]),
     "bfe_plan_create_assembled": (I32, [VP, ctypes.c_double, I32, I32, ctypes.POINTER(VP)]),
+    "bfe_convolve": (I32, [I64, I64, PD, I64, PD, PD]),
+    "bfe_fmc_gather": (I32, [I64, I64, I64, PD, I64, PI64, PI64, PI64, PD, I64, PD, PD]),
+    "bfe_fmc_gather_device": (I32, [I64, I64, I64, VP, I64, PI64, PI64, PI64, PD, I64, PD, VP, VP]),
+    "bfe_disps_to_forces": (I32, [ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
+                                  ctypes.POINTER(BfeSparse), ctypes.c_double, I64, PD, PI32, I32, I32,
+                                  PI64, PI64, PD]),
     "bfe_field_create": (I32, [I32, I32, I64, I64, I32, PD, I32, PI64, I64, I32, PI64, PD,
                                ctypes.POINTER(VP)]),
     "bfe_field_destroy": (I32, [VP]),

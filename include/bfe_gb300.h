@@ -260,6 +260,52 @@ int bfe_plan_create_assembled(const bfe_matrices* m, double dt, int32_t solver_m
                               bfe_plan** out);
 
 /*
+ * Sub-domain and FMC post-processing on the GPU.
+ *
+ * bfe_convolve: code/internal/fn_convolve.m:22-33 along dimension 1. h holds
+ * the first n_t samples of the FFT convolution with 2 n_t points of every
+ * column of f (n_t x n_sig) with g (n_g samples; beyond 2 n_t ignored, as
+ * fft(g, 2 n_t) truncates), evaluated as the equivalent direct sum. Host
+ * buffers, column-major.
+ */
+int bfe_convolve(int64_t n_t, int64_t n_sig, const double* f, int64_t n_g, const double* g, double* h);
+
+/*
+ * fn_parse_to_fmc (subdoms/fn_run_main_model.m:239-256): for pair k,
+ * time_data(:, k) = sum_e rx_w[e] hist(rx_slot[e], :, pair_tx[k]) over
+ * e in [rx_ptr[k], rx_ptr[k+1]) (the receiver's monitored rows of the
+ * transmitter's step, with the receiver's weights or ones), convolved with
+ * in_sig (n_g samples; none if n_g = 0) as bfe_convolve does.
+ *   hist       q x n_t x R (bfe_run_batched's layout)
+ *   time_data  n_t x n_pairs
+ * bfe_fmc_gather takes host buffers; bfe_fmc_gather_device takes device
+ * hist and time_data (index arrays and in_sig stay on the host) and a stream.
+ */
+int bfe_fmc_gather(int64_t q, int64_t n_t, int64_t R, const double* hist, int64_t n_pairs,
+                   const int64_t* pair_tx, const int64_t* rx_ptr, const int64_t* rx_slot, const double* rx_w,
+                   int64_t n_g, const double* in_sig, double* time_data);
+int bfe_fmc_gather_device(int64_t q, int64_t n_t, int64_t R, const double* d_hist, int64_t n_pairs,
+                          const int64_t* pair_tx, const int64_t* rx_ptr, const int64_t* rx_slot,
+                          const double* rx_w, int64_t n_g, const double* in_sig, double* d_time_data,
+                          void* stream);
+
+/*
+ * code/fn_convert_disps_to_forces_v2.m:1-31: forces on the layer-2 and
+ * layer-3 DOFs of a sub-domain that reproduce the displacements disp
+ * (n x n_t, host, column-major): M_lumped accn + C vel + K disp restricted to
+ * those rows, after zeroing the displacements of layers 3, 4 (in_or_out = 0,
+ * 'in') or 1, 2 (in_or_out = 1, 'out'); accn and vel are the differences of
+ * the reference with two leading zero samples, vel per solver_mode, disp
+ * delayed by one sample. lyrs[i] in {0..4} labels DOF i. On return n_force
+ * is the number of force rows, force_rows (n entries available) their
+ * 0-based DOFs in order, and force (n_force x n_t) the forces; force may be
+ * NULL when no DOF is in layers 2 or 3.
+ */
+int bfe_disps_to_forces(const bfe_sparse* K, const bfe_sparse* C, const bfe_sparse* M, double dt, int64_t n_t,
+                        const double* disp, const int32_t* lyrs, int32_t in_or_out, int32_t solver_mode,
+                        int64_t* n_force, int64_t* force_rows, double* force);
+
+/*
  * R independent load steps sharing one operator (array full-matrix capture:
  * one step per transmitter, subdoms/fn_run_main_model.m:101-115), run as one
  * multi-right-hand-side time march. Host buffers.

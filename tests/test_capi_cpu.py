@@ -145,3 +145,15 @@ def test_assembly_argument_errors_are_caught_on_host():
     bad = np.array(m["typ"], dtype=object)
     with pytest.raises(KeyError):
         bfe_gb300.assemble_gpu(mod["nds"], mod["els"], mod["el_mat_i"], None, ["HEX8"] * len(bad), m["matls"])
+
+
+def test_postprocessing_argument_errors_are_caught_on_host():
+    L, lib = _lib()
+    h = np.zeros(4)
+    assert lib.bfe_convolve(0, 1, None, 0, None, None) == L.BFE_ERR_ARG
+    assert lib.bfe_convolve(4, 1, None, 1, None, L.ptr(h, ctypes.c_double)) == L.BFE_ERR_ARG
+    assert lib.bfe_fmc_gather(0, 4, 1, None, 1, None, None, None, None, 0, None, None) == L.BFE_ERR_ARG
+    n_force = ctypes.c_int64()
+    assert lib.bfe_disps_to_forces(None, None, None, 1.0, 4, None, None, 0, 0, ctypes.byref(n_force),
+                                   None, None) == L.BFE_ERR_ARG
+    assert b"NULL" in lib.bfe_last_error()
