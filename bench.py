@@ -366,6 +366,7 @@ def run_ours(args):
 
     extra = {}
     if rank == 0 and not args.no_extra:
+        extra["plate_c0"] = plate_c0_section(bfe_gb300, model)
         extra["fmc_c2a"] = fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, mon_parts[0].size, sig, stream)
         extra["assembly_c1"] = assembly_section(torch, bfe_gb300, model, main)
         extra["hex3d_c3"] = hex3d_section(torch, bfe_gb300, model)
@@ -416,6 +417,42 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+def plate_c0_section(bfe_gb300, model):
+    """The reference's CPU-runnable case: 20 x 10 mm steel plate at 0.1 mm
+    (40,602 DOF, dof_to_use [1 2]), one top-centre point force, 16 top-surface
+    monitors, 2,000 samples, a field frame every 500 samples, through the
+    drop-in v6 call (plan creation, host buffers and copies included), FP64
+    and FP32, against the FP64 C port of the v6 loop on all host threads.
+    The model fits in L2."""
+    from oracle import cpu_port
+    m = model.steel_plate(W=20e-3, H=10e-3, h=0.1e-3, n_mon=16)
+    n_t = 2000
+    t = np.arange(n_t) * m["dt"]
+    sig = model.toneburst(t, 5e6, 5)
+    fi = model.global_indices(m["gl"], m["src_nodes"], 2)
+    hi = model.global_indices(m["gl"], m["mon_nodes"], 2)
+    res = {"n_dof": int(m["K"].shape[0]), "nnz_K": int(m["K"].nnz), "samples": n_t, "l2_resident": True}
+    h64 = None
+    for prec in ("double", "single"):
+        best = 1e30
+        for _ in range(3):
+            t0 = time.perf_counter()
+            h, fld, _, _ = bfe_gb300.fn_explicit_dynamic_solver_gb300(
+                m["K"], m["C"], m["M"], t, fi, sig, [], [], hi, 500, 1, "KE", bfe_gb300.VEL_CURRENT, prec,
+                gl_lookup=m["gl"])
+            best = min(best, time.perf_counter() - t0)
+        res[prec] = {"call_s": best, "dof_updates_per_s": m["K"].shape[0] * n_t / best}
+        if prec == "double":
+            h64 = h
+        else:
+            res[prec]["ascan_err_vs_fp64"] = float(np.abs(h - h64).max() / np.abs(h64).max())
+    op = cpu_port.CpuOperator(m["K"], m["C"], m["M"], m["dt"])
+    _, s = cpu_port.time_march(op, t, fi - 1, sig[None, :], hi - 1)
+    res["cpu_port"] = {"s": s, "dof_updates_per_s": m["K"].shape[0] * n_t / s, "threads": cpu_port.threads()}
+    res["speedup_fp64_call_vs_cpu"] = s / res["double"]["call_s"]
+    return res
 
 
 def fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, n_rx, sig, stream):

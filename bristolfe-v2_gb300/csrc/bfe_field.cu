@@ -34,9 +34,15 @@ __device__ __forceinline__ double frame_value(const T* un, const T* uo, int is_v
 template <typename T>
 __global__ void __launch_bounds__(256) field_kernel(FieldArgs f, const T* __restrict__ un,
                                                     const T* __restrict__ uo, int is_vel, double dt,
-                                                    double* __restrict__ out) {
+                                                    double* __restrict__ out, const int64_t* ti_dev,
+                                                    int64_t ti, int64_t every) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= f.n_el) return;
+  if (every > 0) {                             // inside a march: frame steps only
+    const int64_t step = ti_dev ? *ti_dev + ti : ti;
+    if (step % every) return;
+    out += f.n_el * (step / every);
+  }
   const int32_t* en = f.els + e * f.el_cols;
   double acc = 0.0;
   int used = 0;
@@ -79,18 +85,26 @@ __global__ void __launch_bounds__(256) field_kernel(FieldArgs f, const T* __rest
   out[e] = acc;
 }
 
-cudaError_t launch_field(const FieldArgs& f, const void* u_new, const void* u_old, int precision,
-                         int is_vel, double dt, double* out, cudaStream_t st) {
+cudaError_t launch_field_step(const FieldArgs& f, const void* u_new, const void* u_old, int precision,
+                              int is_vel, double dt, double* out, const int64_t* ti_dev, int64_t ti,
+                              int64_t every, cudaStream_t st) {
   if (f.n_el == 0) return cudaSuccess;
   const int threads = 256;
   const unsigned blocks = (unsigned)((f.n_el + threads - 1) / threads);
   if (precision == 0)
     field_kernel<double><<<blocks, threads, 0, st>>>(f, static_cast<const double*>(u_new),
-                                                     static_cast<const double*>(u_old), is_vel, dt, out);
+                                                     static_cast<const double*>(u_old), is_vel, dt, out,
+                                                     ti_dev, ti, every);
   else
     field_kernel<float><<<blocks, threads, 0, st>>>(f, static_cast<const float*>(u_new),
-                                                    static_cast<const float*>(u_old), is_vel, dt, out);
+                                                    static_cast<const float*>(u_old), is_vel, dt, out,
+                                                    ti_dev, ti, every);
   return cudaGetLastError();
+}
+
+cudaError_t launch_field(const FieldArgs& f, const void* u_new, const void* u_old, int precision,
+                         int is_vel, double dt, double* out, cudaStream_t st) {
+  return launch_field_step(f, u_new, u_old, precision, is_vel, dt, out, nullptr, 0, 0, st);
 }
 
 }  // namespace bfe

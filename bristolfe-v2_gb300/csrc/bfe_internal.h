@@ -69,7 +69,23 @@ struct StepArgs {
   int64_t ti;                 // 0-based time index of the computed state, or (when
                               // ti_dev is set) its offset from *ti_dev
   const int64_t* ti_dev;      // device time-index base (graph replay) or nullptr
+  // field frames written by the one-source kernels themselves (R = 1): on
+  // steps with ti % fld_every == 0, fld[i + n * (ti / fld_every)] =
+  // (u_new - u_n) / dt (fld_is_vel) or u_new; nullptr = none
+  double* fld;
+  int64_t fld_every;
+  int32_t fld_is_vel;
+  double dt;
 };
+
+// Frame value of row i on a frame step (one-source kernels).
+template <typename T>
+__device__ __forceinline__ void write_frame(const StepArgs& a, int i, T unew, T un) {
+  const int64_t ti = a.ti_dev ? *a.ti_dev + a.ti : a.ti;
+  if (ti % a.fld_every) return;
+  a.fld[(size_t)i + (size_t)a.n * (size_t)(ti / a.fld_every)] =
+      a.fld_is_vel ? ((double)unew - (double)un) / a.dt : (double)unew;
+}
 
 // Time index of the state a kernel computes.
 __device__ __forceinline__ int64_t step_index(const StepArgs& a) {
@@ -200,6 +216,12 @@ struct FieldArgs {
 // u of the plan's precision (0: double, 1: float).
 cudaError_t launch_field(const FieldArgs& f, const void* u_new, const void* u_old, int precision,
                          int is_vel, double dt, double* out, cudaStream_t s);
+// The same inside a time march: the kernel takes the step index from
+// *ti_dev + ti (ti_dev may be nullptr) and writes out + n_el * (ti / every)
+// on frame steps only, so it can be captured in a graph.
+cudaError_t launch_field_step(const FieldArgs& f, const void* u_new, const void* u_old, int precision,
+                              int is_vel, double dt, double* out, const int64_t* ti_dev, int64_t ti,
+                              int64_t every, cudaStream_t s);
 const FieldArgs& field_args(const bfe_field* f);
 int64_t field_ndof(const bfe_field* f);
 int field_device(const bfe_field* f);

@@ -89,9 +89,10 @@ __global__ void __launch_bounds__(256) step_f64_r1(StepArgs a) {
   if (info & kRowInterface) {
     const int t = lower_bound_i32(a.int_row, a.n_int, i);
     static_cast<double*>(a.v_int)[t] = a.int_base_prev ? (r - up) : (un[i] - up);
-  } else if (info & kRowMonitored) {
-    write_history(a, i, 0, r);
+    return;
   }
+  if (info & kRowMonitored) write_history(a, i, 0, r);
+  if (a.fld) write_frame<double>(a, i, r, un[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -128,9 +129,10 @@ __global__ void __launch_bounds__(256) step_f32_r1(StepArgs a) {
   if (info & kRowInterface) {
     const int t = lower_bound_i32(a.int_row, a.n_int, i);
     static_cast<float*>(a.v_int)[t] = a.int_base_prev ? (d + err + inc) : (d + err);
-  } else if (info & kRowMonitored) {
-    write_history(a, i, 0, (double)r);
+    return;
   }
+  if (info & kRowMonitored) write_history(a, i, 0, (double)r);
+  if (a.fld) write_frame<float>(a, i, r, ui);
 }
 
 // ---------------------------------------------------------------------------
@@ -1025,6 +1027,7 @@ __global__ void __launch_bounds__(256) interface_fixup_r1(StepArgs a) {
     const T r = base + acc;
     unew[row] = r;
     if (__ldg(a.rowinfo + row) & kRowMonitored) write_history(a, row, 0, (double)r);
+    if (a.fld) write_frame<T>(a, row, r, static_cast<const T*>(a.u_n)[row]);
   }
 }
 

@@ -1167,6 +1167,23 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   }
   stt.variant = variant;
   int v5_flip = 0;
+  // Field frames: the one-source kernels write raw frames themselves, an
+  // element field is reduced by a kernel that checks the step on the device;
+  // both can be captured in a graph. The v5 rows patch frames per step from
+  // the host (no graph then). Frame times are known up front: frames before
+  // the first forced sample stay zero with time zero (v6.m:163-169,200-208).
+  const bool frames = rs.every_n > 0 && (rs.d_fld || rs.field);
+  const bool fused_frames = frames && rs.d_fld && !rs.field && R == 1 && !rs.v5;
+  if (fused_frames) {
+    a.fld = rs.d_fld;
+    a.fld_every = rs.every_n;
+    a.fld_is_vel = rs.field_is_vel;
+    a.dt = pl->dt;
+  }
+  if (frames && rs.fld_time)
+    for (int64_t k = 0; k * rs.every_n < rs.n_t; ++k)
+      if (k * rs.every_n >= rs.ti_start) (*rs.fld_time)[k] = rs.time[k * rs.every_n];
+  bool capturing = false;
   // One time step: step kernel, interface correction, optional frame, v5 rows.
   auto one_step = [&](int64_t ti, bool rec) -> int {
     a.u_prev = U[iprev];
@@ -1185,19 +1202,21 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       stt.aux_launches++;
     }
     double* frame_col = nullptr;
-    if (ti >= 0 && rs.every_n > 0 && (rs.d_fld || rs.field) && ti % rs.every_n == 0) {
+    if (rs.field && (capturing || ti % rs.every_n == 0)) {
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
+      e = bfe::launch_field_step(*rs.field, a.u_new, a.u_n, prec, rs.field_is_vel, pl->dt, rs.d_el,
+                                 a.ti_dev, a.ti, rs.every_n, st);
+      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "field kernel launch failed: %s", cudaGetErrorString(e));
+      if (rec && timing) CUDA_TRY(mark(ev_aux));
+      stt.aux_launches++;
+    } else if (frames && !fused_frames && !rs.field && ti % rs.every_n == 0) {
       const int64_t k = ti / rs.every_n;
       if (rec && timing) CUDA_TRY(mark(ev_aux));
-      if (rs.field)
-        e = bfe::launch_field(*rs.field, a.u_new, a.u_n, prec, rs.field_is_vel, pl->dt,
-                              rs.d_el + (size_t)rs.field->n_el * k, st);
-      else
-        e = bfe::launch_frame(a, prec, rs.d_fld, k, rs.field_is_vel, pl->dt, st);
+      e = bfe::launch_frame(a, prec, rs.d_fld, k, rs.field_is_vel, pl->dt, st);
       if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "frame kernel launch failed: %s", cudaGetErrorString(e));
       if (rec && timing) CUDA_TRY(mark(ev_aux));
       stt.aux_launches++;
-      if (rs.fld_time) (*rs.fld_time)[k] = rs.time[ti];
-      if (rs.d_fld) frame_col = rs.d_fld + (size_t)n * k;
+      frame_col = rs.d_fld + (size_t)n * k;
     }
     if (rs.v5) {
       bfe::V5Args v = *rs.v5;
@@ -1222,9 +1241,9 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   // multiple of the 3-buffer state rotation and of the 2-buffer v5 velocity
   // swap) are captured once, with the time index
   // read from a device counter that the last node advances, and replayed.
-  // Not used with per-launch timing, field frames or the legacy stream.
+  // Not used with per-launch timing, v5 frames or the legacy stream.
   const int64_t kGraphSteps = 48;
-  const bool use_graph = !timing && rs.every_n <= 0 && st != nullptr && st != cudaStreamLegacy &&
+  const bool use_graph = !timing && !(rs.v5 && frames) && st != nullptr && st != cudaStreamLegacy &&
                          (rs.n_t - rs.ti_start) >= 2 * kGraphSteps && getenv("BFE_NO_GRAPH") == nullptr;
   DevBuf<int64_t> d_ti;
   cudaGraph_t graph = nullptr;
@@ -1242,10 +1261,12 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     a.ti_dev = d_ti.p;
     const int64_t launches0 = stt.step_launches, aux0 = stt.aux_launches;
     int rc2 = BFE_OK;
+    capturing = true;
     for (int64_t k = 0; k < kGraphSteps && rc2 == BFE_OK; ++k) {
       a.ti = k;
       rc2 = one_step(-1, false);
     }
+    capturing = false;
     if (rc2 == BFE_OK && bfe::launch_advance(d_ti.p, kGraphSteps, st) != cudaSuccess)
       rc2 = fail(BFE_ERR_CUDA, "graph capture failed");
     cudaGraph_t g = nullptr;

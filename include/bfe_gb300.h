@@ -39,7 +39,8 @@ extern "C" {
 #define BFE_ERR_ARG 1          /* invalid argument (sizes, indices, strings) */
 #define BFE_ERR_OOM 2          /* host or device allocation failed */
 #define BFE_ERR_CUDA 3         /* CUDA runtime error */
-#define BFE_ERR_NUMERIC 4      /* zero lumped mass, NaN/Inf in inputs */
+#define BFE_ERR_NUMERIC 4      /* zero lumped mass, NaN/Inf in K, C or M (non-finite signals
+                                  propagate into the outputs, as in the reference) */
 #define BFE_ERR_UNSUPPORTED 5  /* valid request the reference path rejects */
 #define BFE_ERR_NO_DEVICE 6    /* no usable GPU */
 
