@@ -1,5 +1,6 @@
 // Internal declarations shared by the host plan code and the CUDA kernels.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -248,6 +249,29 @@ cudaError_t launch_grad(const GradArgs& g, int precision, cudaStream_t s);
 
 // Message returned by bfe_last_error() on the calling thread.
 void set_last_error(const char* msg);
+
+// Number of SMs of the current device (queried once per device, thread-safe).
+inline int sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int c = (dev >= 0 && dev < 64) ? cache[dev].load(std::memory_order_relaxed) : 0;
+  if (c == 0) {
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    if (dev >= 0 && dev < 64) cache[dev].store(c, std::memory_order_relaxed);
+  }
+  return c;
+}
+
+// True the first time it is called for the current device with this flag
+// set (for per-device, per-function attributes; thread-safe).
+inline bool first_on_device(std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return true;
+  const uint64_t bit = 1ull << dev;
+  return (done.fetch_or(bit) & bit) == 0;
+}
 
 size_t tma_smem_bytes();
 // tm_un / tm_up: CUtensorMap (2D FP32 [n][R], box 64 x 1) of u_n and u_{n-1}.

@@ -1177,18 +1177,16 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
       launch_group2<3>(a, *gr, variant >= 16 ? 14 : variant, st);
     }
   } else if (a.R % 64 == 0 && variant == 8 && gr) {
-    static int sm_count = 0;
-    if (sm_count == 0) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
-      cudaFuncSetAttribute(step_f32_group_async, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)async_smem_bytes());
+    static std::atomic<uint64_t> attr_set{0};
+    if (first_on_device(attr_set)) {
+      const cudaError_t e = cudaFuncSetAttribute(step_f32_group_async, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)async_smem_bytes());
+      if (e != cudaSuccess) return e;
     }
     long n_items = 0;
     for (int k = 0; k < gr->n_groups; ++k) n_items += gr->n_nodes[k];
     n_items *= a.R / 64;
-    step_f32_group_async<<<sm_count * 2, kAsyncWarps * 32, async_smem_bytes(), st>>>(a, *gr, n_items);
+    step_f32_group_async<<<sm_count() * 2, kAsyncWarps * 32, async_smem_bytes(), st>>>(a, *gr, n_items);
   } else if (a.R % 64 == 0 && (variant == 6 || variant == 7) && gr) {
     const int grid = gr->blk_begin[gr->n_groups];
     if (variant == 6) step_f32_group<2><<<grid, threads, 0, st>>>(a, *gr);

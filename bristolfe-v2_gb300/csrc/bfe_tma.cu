@@ -308,11 +308,8 @@ size_t tma_smem_bytes() { return (size_t)kTmaWarps * 2 * kTStageBytes; }
 cudaError_t launch_step_tma(const StepArgs& a, const GroupArgs& gr, const TmaArgs& t,
                             const struct CUtensorMap_st* tm_un, const struct CUtensorMap_st* tm_up,
                             cudaStream_t st) {
-  static int sm_count = 0;
-  if (sm_count == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+  static std::atomic<uint64_t> attr_set{0};
+  if (first_on_device(attr_set)) {
     cudaError_t e = cudaFuncSetAttribute(step_f32_group_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tma_smem_bytes());
     if (e != cudaSuccess) return e;
@@ -320,7 +317,7 @@ cudaError_t launch_step_tma(const StepArgs& a, const GroupArgs& gr, const TmaArg
   long n_items = 0;
   for (int k = 0; k < gr.n_groups; ++k) n_items += gr.n_nodes[k];
   n_items *= a.R / 64;
-  step_f32_group_tma<<<sm_count * 4, kTmaWarps * 32, tma_smem_bytes(), st>>>(a, gr, t, *tm_un, *tm_up, n_items);
+  step_f32_group_tma<<<sm_count() * 4, kTmaWarps * 32, tma_smem_bytes(), st>>>(a, gr, t, *tm_un, *tm_up, n_items);
   return cudaGetLastError();
 }
 
