@@ -146,6 +146,8 @@ struct TmaArgs {
 cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
 // Number of kernel variants the autotuner may choose from for (precision, R).
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups);
+// Whether variant v applies to (precision, R) (the autotuner skips the others).
+bool batched_variant_supported(int precision, int R, int variant, bool have_nodes, bool have_groups);
 cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const GroupArgs* gr,
                                 int precision, int max_slice_entries, int variant,
                                 cudaStream_t s);                                      // any R

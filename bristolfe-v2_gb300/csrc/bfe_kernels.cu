@@ -904,7 +904,7 @@ __device__ __forceinline__ void group4_nbr(const float* nb, const float2* coef, 
   }
 }
 
-template <int BS, int UNROLL, bool LATE_UP, bool RAW>
+template <int BS, int UNROLL, bool LATE_UP, bool RAW, int LPN>
 __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& gr, int gi, int node,
                                             int l16) {
   const int4 rec = __ldg(gr.rec[gi] + node);
@@ -915,7 +915,7 @@ __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& 
   const int32_t* nrow = gr.nrow[gi];
   const float2* coef = gr.coef2[gi];
   const float* craw = gr.coef[gi];
-  for (int c = l16 * 4; c < R; c += 64) {
+  for (int c = l16 * 4; c < R; c += 4 * LPN) {
     float4 uo[BS], up[BS], acc[BS];
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
@@ -968,18 +968,41 @@ __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& 
   }
 }
 
-// 128 threads = 8 half-warps = the 8 nodes of one CTA of the group layout.
-template <int UNROLL, int MINB, bool LATE_UP, bool RAW>
+// 128 threads = 128 / LPN nodes of LPN lanes each (LPN = 16 for R a
+// multiple of 64, 8 for R = 32, 4 for R = 16); gr.blk_begin must hold the
+// CTA ranges for 128 / LPN nodes per CTA.
+template <int UNROLL, int MINB, bool LATE_UP, bool RAW, int LPN = 16>
 __global__ void __launch_bounds__(128, MINB) step_f32_group4(StepArgs a, GroupArgs gr) {
   const int b = blockIdx.x;
   int gi = 0;
 #pragma unroll
   for (int k = 1; k < kMaxGroups; ++k)
     if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
-  const int node = (b - gr.blk_begin[gi]) * 8 + (threadIdx.x >> 4);
+  const int node = (b - gr.blk_begin[gi]) * (128 / LPN) + threadIdx.x / LPN;
   if (node >= gr.n_nodes[gi]) return;
-  if (gr.bs[gi] == 1) group4_node<1, UNROLL * 2, LATE_UP, RAW>(a, gr, gi, node, threadIdx.x & 15);
-  else group4_node<2, UNROLL, LATE_UP, RAW>(a, gr, gi, node, threadIdx.x & 15);
+  if (gr.bs[gi] == 1) group4_node<1, UNROLL * 2, LATE_UP, RAW, LPN>(a, gr, gi, node, threadIdx.x % LPN);
+  else group4_node<2, UNROLL, LATE_UP, RAW, LPN>(a, gr, gi, node, threadIdx.x % LPN);
+}
+
+// The variants of the half-warp family for lanes-per-node LPN.
+template <int LPN>
+static void launch_group4(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {
+  GroupArgs g = gr;
+  int blocks = 0;
+  for (int k = 0; k < g.n_groups; ++k) {
+    g.blk_begin[k] = blocks;
+    blocks += (g.n_nodes[k] + 128 / LPN - 1) / (128 / LPN);
+  }
+  g.blk_begin[g.n_groups] = blocks;
+  switch (variant) {
+    case 16: step_f32_group4<1, 10, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
+    case 17: step_f32_group4<2, 8, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
+    case 18: step_f32_group4<1, 12, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
+    case 19: step_f32_group4<1, 12, true, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
+    case 20: step_f32_group4<1, 12, false, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
+    case 21: step_f32_group4<1, 12, true, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
+    default: step_f32_group4<1, 10, false, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1127,14 +1150,22 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 // 9, 10, 11 = packed-math group kernel (unroll 1, 2, 4), 12-14 = the same
 // with occupancy hints of 4, 6 and 8 resident CTAs.
 // 15 = TMA-staged group kernel (bfe_tma.cu; launched by the plan code).
-// 16-22 = half-warp-per-node float4 group kernel: 16 unroll 1 at occupancy
+// 16-22 = half-warp-per-node float4 group kernel (4 or 8 lanes per node for
+// R = 16 or 32, where only variants 0 and 16-22 apply): 16 unroll 1 at occupancy
 // hint 10 CTAs of 128 threads, 17 unroll 2 at 8, 18 unroll 1 at 12, 19 the
 // same with u_{n-1} read in the epilogue, 20-22 with one 16-byte load of each
 // block's coefficients (hint 12, 12 with the late u_{n-1}, 10); block sizes
 // <= 2 (3D plans fall back to variant 14).
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
   if (precision == 1 && R % 64 == 0) return have_groups ? 23 : (have_nodes ? 6 : 4);
+  if (precision == 1 && (R == 16 || R == 32) && have_groups) return 23;
   return 1;
+}
+
+bool batched_variant_supported(int precision, int R, int variant, bool have_nodes, bool have_groups) {
+  if (variant >= batched_variants(precision, R, have_nodes, have_groups)) return false;
+  if (precision == 1 && (R == 16 || R == 32)) return variant == 0 || variant >= 16;
+  return true;
 }
 
 template <int MAXBS>
@@ -1157,20 +1188,23 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
+  } else if ((a.R == 16 || a.R == 32) && variant >= 16 && variant <= 22 && gr) {
+    int maxbs = 1;
+    for (int k = 0; k < gr->n_groups; ++k) maxbs = gr->bs[k] > maxbs ? gr->bs[k] : maxbs;
+    if (maxbs > 2) {
+      step_batched<float, 1><<<a.n_slices, threads, smem, st>>>(a);
+    } else if (a.R == 32) {
+      launch_group4<8>(a, *gr, variant, st);
+    } else {
+      launch_group4<4>(a, *gr, variant, st);
+    }
   } else if (a.R % 64 == 0 && variant >= 9 && variant <= 22 && gr) {
     int maxbs = 1;
     for (int k = 0; k < gr->n_groups; ++k) maxbs = gr->bs[k] > maxbs ? gr->bs[k] : maxbs;
-    const int grid = gr->blk_begin[gr->n_groups];
     if (variant >= 16 && maxbs <= 2) {
-      switch (variant) {
-        case 16: step_f32_group4<1, 10, false, false><<<grid, 128, 0, st>>>(a, *gr); break;
-        case 17: step_f32_group4<2, 8, false, false><<<grid, 128, 0, st>>>(a, *gr); break;
-        case 18: step_f32_group4<1, 12, false, false><<<grid, 128, 0, st>>>(a, *gr); break;
-        case 19: step_f32_group4<1, 12, true, false><<<grid, 128, 0, st>>>(a, *gr); break;
-        case 20: step_f32_group4<1, 12, false, true><<<grid, 128, 0, st>>>(a, *gr); break;
-        case 21: step_f32_group4<1, 12, true, true><<<grid, 128, 0, st>>>(a, *gr); break;
-        default: step_f32_group4<1, 10, false, true><<<grid, 128, 0, st>>>(a, *gr); break;
-      }
+      if (a.R % 64 == 0) launch_group4<16>(a, *gr, variant, st);
+      else if (a.R == 32) launch_group4<8>(a, *gr, variant, st);
+      else launch_group4<4>(a, *gr, variant, st);
     } else if (maxbs <= 2) {
       launch_group2<2>(a, *gr, variant >= 16 ? 14 : variant, st);
     } else {

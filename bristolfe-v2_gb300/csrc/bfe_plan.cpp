@@ -1145,6 +1145,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       float best = 1e30f;
       for (int v = 0; v < nv; ++v) {
         if (v == 15 && !have_tmaps) continue;
+        if (!bfe::batched_variant_supported(prec, (int)R, v, pl->have_node_blocks, pl->have_groups)) continue;
         CUDA_TRY(launch_batched(gp, grp, v, 1, 0));   // warm
         CUDA_TRY(cudaEventRecord(e0, st));
         for (int k = 0; k < 3; ++k) CUDA_TRY(launch_batched(gp, grp, v, 1, 0));
@@ -1831,12 +1832,18 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   RunArrays rf;
   bfe::StepArgs af;
   if ((rc = prepare_run(pl, frc, hidx, R, n_t, n_sig, d_sig.p, d_hist.p, st, rf, af))) return rc;
-  const bool use_groups = R % 64 == 0 && pl->have_groups && prec == BFE_PREC_SINGLE;
+  const bool use_groups = (R % 64 == 0 || R == 16 || R == 32) && pl->have_groups && prec == BFE_PREC_SINGLE;
   const bfe::GroupArgs* grp = use_groups ? &pl->groups : nullptr;
+  // the variant the forward runs chose for this R, else the half-warp kernel
+  // (raw coefficients; 3D plans map it to the warp-per-node kernel)
+  int variant = use_groups ? 20 : 0;
+  if (use_groups) {
+    auto it = pl->variant_of_R.find(R);
+    if (it != pl->variant_of_R.end()) variant = it->second;
+  }
   auto step = [&](bfe::StepArgs& a) -> int {
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, nullptr, grp, prec, pl->max_slice_entries,
-                                                      use_groups ? 14 : 0, st);
+                           : bfe::launch_step_batched(a, nullptr, grp, prec, pl->max_slice_entries, variant, st);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (pl->n_int) {
       e = bfe::launch_interface_fixup(a, prec, st);

@@ -136,3 +136,22 @@ def test_autograd_wrapper_gradient(bfe, problem):
     assert float(J.detach()) == pytest.approx(J_ref, rel=1e-12)
     assert np.allclose(s.grad.numpy(), gs, rtol=1e-10, atol=1e-30)
     assert np.allclose(rho.grad.numpy(), gr, rtol=1e-10, atol=1e-40)
+
+
+def test_fp32_adjoint_with_16_sources_matches_fp64(bfe, problem):
+    """16 sources take the 4-lanes-per-node FP32 kernels in the forward,
+    recompute and adjoint marches; FP32 and FP64 gradients agree."""
+    P = problem
+    ke, mh, ch, dof = P["ed"]
+    top = P["m"]["mon_nds"]
+    srcs = [modelgen.gi_of(P["m"]["gl"], [top[k % top.size]], 1 + (k // top.size) % 2) for k in range(16)]
+    obs = np.zeros((P["hi1"].size, P["t"].size, 16))
+    obs[:, :, :2] = P["obs"]
+    out = {}
+    for prec in ("double", "single"):
+        with _plan(bfe, P, prec) as plan:
+            out[prec] = plan.adjoint_gradient((ke, mh, ch, dof), P["t"], srcs, P["sig"], P["hi1"], obs)
+    (J64, gs64, gr64), (J32, gs32, gr32) = out["double"], out["single"]
+    assert abs(J32 - J64) <= 1e-4 * J64
+    assert np.linalg.norm(gs32 - gs64) <= 1e-4 * np.linalg.norm(gs64)
+    assert np.linalg.norm(gr32 - gr64) <= 1e-4 * np.linalg.norm(gr64)

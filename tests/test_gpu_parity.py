@@ -200,6 +200,26 @@ def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
         assert _err(hb[q4:, :, r], h0[q4:]) <= TOL32
 
 
+@pytest.mark.parametrize("R", [16, 32])
+@pytest.mark.parametrize("variant", [0] + list(range(16, 23)))
+def test_half_warp_kernels_with_16_and_32_sources(bfe, coupled, R, variant, monkeypatch):
+    """The half-warp group kernels with 4 (R = 16) or 8 (R = 32) lanes per
+    node, and the slice kernel, against the oracle."""
+    m = coupled
+    nt = 150
+    t, s = modelgen.pulse(nt, m["dt"])
+    nds = np.nonzero(m["gl"][:, 3] > 0)[0] + 1
+    srcs = [modelgen.gi_of(m["gl"], [nds[(13 * r) % nds.size]], 4) for r in range(R)]
+    hi = np.concatenate([modelgen.gi_of(m["gl"], m["mon_nds"], 4), modelgen.gi_of(m["gl"], m["mon_nds"], 2)])
+    monkeypatch.setenv("BFE_VARIANT", str(variant))
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, "single", m["gl"]) as plan:
+        hb = plan.run_batched(t, srcs, s, hi)
+        assert plan.stats()["variant"] == variant
+    for r in (0, R - 1):
+        h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
+        assert _err(hb[:, :, r], h0) <= TOL32
+
+
 @pytest.mark.parametrize("prec,tol", [("double", TOL64), ("single", TOL32)])
 def test_multi_model_plan_matches_each_model(bfe, plate, coupled, prec, tol):
     """Independent models joined block-diagonally in one plan: each model's
