@@ -130,6 +130,7 @@ struct GroupArgs {
   const int32_t* frow[kMaxGroups];   // flat neighbour rows: BS rows per neighbour block
   const float2* coef2[kMaxGroups];   // the coefficients as broadcast pairs {c, c}
   const int4* rec[kMaxGroups];       // per node {first row, first neighbour block, neighbour count, 0}
+  const double* coef64[kMaxGroups];  // FP64 plans: B per block (own block included), [own k][l]
 };
 
 // Extra data of the TMA-staged group kernel (bfe_tma.cu): per node the

@@ -1005,6 +1005,123 @@ static void launch_group4(const StepArgs& a, const GroupArgs& gr, int variant, c
   }
 }
 
+// FP64 group block-sparse kernel (direct form, the reference's arithmetic):
+// u_new = sum over the node's blocks (its own included) of B_block u_n
+// + D u_{n-1} + forcing, summed in column order like the one-source kernel.
+// LPN lanes per node, VEC doubles (right-hand sides) per lane and pass.
+template <int BS, int LPN, int VEC>
+__device__ __forceinline__ void group64_node(const StepArgs& a, const GroupArgs& gr, int gi, int node,
+                                             int lane) {
+  const int4 rec = __ldg(gr.rec[gi] + node);
+  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
+  const int R = a.R;
+  const size_t rs = (size_t)R;
+  const double* un = static_cast<const double*>(a.u_n);
+  const int32_t* nrow = gr.nrow[gi];
+  const double* cf = gr.coef64[gi];
+  for (int c = lane * VEC; c < R; c += LPN * VEC) {
+    double acc[BS][VEC];
+#pragma unroll
+    for (int k = 0; k < BS; ++k)
+#pragma unroll
+      for (int v = 0; v < VEC; ++v) acc[k][v] = 0.0;
+    for (int e = p0; e < p1; ++e) {
+      const double* nb = un + (size_t)__ldg(nrow + e) * rs + c;
+      double g[BS][VEC];
+#pragma unroll
+      for (int l = 0; l < BS; ++l)
+#pragma unroll
+        for (int v = 0; v < VEC; v += 2) {
+          const double2 x = __ldg(reinterpret_cast<const double2*>(nb + l * rs + v));
+          g[l][v] = x.x;
+          g[l][v + 1] = x.y;
+        }
+      double cv[BS * BS];
+#pragma unroll
+      for (int t = 0; t < BS * BS; ++t) cv[t] = __ldg(cf + (size_t)e * (BS * BS) + t);
+#pragma unroll
+      for (int l = 0; l < BS; ++l)
+#pragma unroll
+        for (int k = 0; k < BS; ++k)
+#pragma unroll
+          for (int v = 0; v < VEC; ++v) acc[k][v] = fma(cv[k * BS + l], g[l][v], acc[k][v]);
+    }
+    double* unew = static_cast<double*>(a.u_new);
+    const double* upv = static_cast<const double*>(a.u_prev);
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      const int row = row0 + k;
+      const uint32_t info = __ldg(a.rowinfo + row);
+      const double dk = __ldg(static_cast<const double*>(a.rowc) + row);
+      const size_t o = (size_t)row * rs + c;
+      double res[VEC], upk[VEC];
+#pragma unroll
+      for (int v = 0; v < VEC; v += 2) {
+        const double2 x = __ldcs(reinterpret_cast<const double2*>(upv + o + v));
+        upk[v] = x.x;
+        upk[v + 1] = x.y;
+      }
+#pragma unroll
+      for (int v = 0; v < VEC; ++v) {
+        double r = acc[k][v] + dk * upk[v];
+        if (info & kRowForced) r += forcing_sum<double>(a, row, c + v);
+        res[v] = r;
+      }
+#pragma unroll
+      for (int v = 0; v < VEC; v += 2)
+        *reinterpret_cast<double2*>(unew + o + v) = make_double2(res[v], res[v + 1]);
+      if (info & kRowInterface) {
+        const int t = lower_bound_i32(a.int_row, a.n_int, row);
+        double* vi = static_cast<double*>(a.v_int) + (size_t)t * R + c;
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) vi[v] = a.int_base_prev ? (res[v] - upk[v]) : (un[o + v] - upk[v]);
+      } else if (info & kRowMonitored) {
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) write_history(a, row, c + v, res[v]);
+      }
+    }
+  }
+}
+
+template <int LPN, int VEC, int MINB, int MAXBS>
+__global__ void __launch_bounds__(128, MINB) step_f64_group(StepArgs a, GroupArgs gr) {
+  const int b = blockIdx.x;
+  int gi = 0;
+#pragma unroll
+  for (int k = 1; k < kMaxGroups; ++k)
+    if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
+  const int node = (b - gr.blk_begin[gi]) * (128 / LPN) + threadIdx.x / LPN;
+  if (node >= gr.n_nodes[gi]) return;
+  if (gr.bs[gi] == 1) group64_node<1, LPN, VEC>(a, gr, gi, node, threadIdx.x % LPN);
+  else if (MAXBS == 2 || gr.bs[gi] == 2) group64_node<(MAXBS >= 2 ? 2 : 1), LPN, VEC>(a, gr, gi, node, threadIdx.x % LPN);
+  else group64_node<MAXBS, LPN, VEC>(a, gr, gi, node, threadIdx.x % LPN);
+}
+
+// FP64 variants: 1 = 16 lanes x 4 right-hand sides (R a multiple of 64),
+// 2 = 16 x 2 (R a multiple of 32), 3 = 8 x 2 (R a multiple of 16).
+static cudaError_t launch_group64(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {
+  const int lpn = variant == 3 ? 8 : 16;
+  GroupArgs g = gr;
+  int blocks = 0;
+  for (int k = 0; k < g.n_groups; ++k) {
+    g.blk_begin[k] = blocks;
+    blocks += (g.n_nodes[k] + 128 / lpn - 1) / (128 / lpn);
+  }
+  g.blk_begin[g.n_groups] = blocks;
+  int maxbs = 1;
+  for (int k = 0; k < g.n_groups; ++k) maxbs = g.bs[k] > maxbs ? g.bs[k] : maxbs;
+  if (maxbs <= 2) {
+    if (variant == 1) step_f64_group<16, 4, 8, 2><<<blocks, 128, 0, st>>>(a, g);
+    else if (variant == 2) step_f64_group<16, 2, 10, 2><<<blocks, 128, 0, st>>>(a, g);
+    else step_f64_group<8, 2, 10, 2><<<blocks, 128, 0, st>>>(a, g);
+  } else {
+    if (variant == 1) step_f64_group<16, 4, 6, 3><<<blocks, 128, 0, st>>>(a, g);
+    else if (variant == 2) step_f64_group<16, 2, 8, 3><<<blocks, 128, 0, st>>>(a, g);
+    else step_f64_group<8, 2, 8, 3><<<blocks, 128, 0, st>>>(a, g);
+  }
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
@@ -1142,7 +1259,9 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
   return ((size_t(max_slice_entries) * 4 + 15) & ~size_t(15)) + size_t(max_slice_entries) * elem;
 }
 
-// Variants for the autotuner. FP32 with R % 64 == 0: 0 = slice-staged
+// Variants for the autotuner. FP64 with group arrays and R % 16 == 0: 0 =
+// slice-staged rows, 1-3 = the FP64 group kernel (launch_group64). FP32
+// with R % 64 == 0: 0 = slice-staged
 // row kernel, 1..3 = half-warp float4 row kernels, 4 = node-block kernel
 // (only when the plan has node blocks), 5 = node-block kernel, deeper unroll.
 // 6, 7 = group block-sparse kernel (unroll 2, 4), 8 = group block-sparse
@@ -1159,12 +1278,15 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 int batched_variants(int precision, int R, bool have_nodes, bool have_groups) {
   if (precision == 1 && R % 64 == 0) return have_groups ? 23 : (have_nodes ? 6 : 4);
   if (precision == 1 && (R == 16 || R == 32) && have_groups) return 23;
+  if (precision == 0 && R % 16 == 0 && have_groups) return 4;
   return 1;
 }
 
 bool batched_variant_supported(int precision, int R, int variant, bool have_nodes, bool have_groups) {
   if (variant >= batched_variants(precision, R, have_nodes, have_groups)) return false;
   if (precision == 1 && (R == 16 || R == 32)) return variant == 0 || variant >= 16;
+  if (precision == 0) return variant == 0 || (variant == 1 && R % 64 == 0) || (variant == 2 && R % 32 == 0) ||
+                             variant == 3;
   return true;
 }
 
@@ -1187,6 +1309,7 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
   const int threads = 256;
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
+    if (variant >= 1 && variant <= 3 && gr) return launch_group64(a, *gr, variant, st);
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
   } else if ((a.R == 16 || a.R == 32) && variant >= 16 && variant <= 22 && gr) {
     int maxbs = 1;

@@ -268,6 +268,7 @@ struct bfe_plan {
   DevBuf<int> d_err;
   bfe::TmaArgs tma{};
   DevBuf<float> g_coef[bfe::kMaxGroups];
+  DevBuf<double> g_coef64[bfe::kMaxGroups];
   // BFE_MODE_V5: K, C (FP64 CSR) and the lumped mass, for the
   // prescribed-displacement rows of bfe_run_v5
   Csr hK, hC;
@@ -475,21 +476,27 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
     }
   }
 
-  // node blocks for the FP32 difference form
+  // node blocks (consecutive rows of one node): the FP32 difference form and
+  // the group block-sparse operators of both precisions use them
   std::vector<int64_t> blk_base(n, -1), blk_len(n, 0);
-  bool have_nodes = precision == BFE_PREC_SINGLE && dof_node && dof_type;
-  if (have_nodes) {
+  bool nodes_ok = dof_node && dof_type;
+  if (nodes_ok) {
     int64_t i = 0;
     std::map<int64_t, int64_t> seen;
-    while (i < n && have_nodes) {
+    while (i < n && nodes_ok) {
       int64_t j = i;
       while (j < n && dof_node[j] == dof_node[i]) ++j;
-      if (j - i > 8 || seen.count(dof_node[i])) { have_nodes = false; break; }
+      if (j - i > 8 || seen.count(dof_node[i])) { nodes_ok = false; break; }
       seen[dof_node[i]] = i;
       for (int64_t k = i; k < j; ++k) { blk_base[k] = i; blk_len[k] = j - i; }
       i = j;
     }
   }
+  const bool have_nodes = precision == BFE_PREC_SINGLE && nodes_ok;
+  // diagonal term of B in the FP64 form (v6.m:131-138 with the diagonal of P)
+  auto diag_term = [&](int64_t i) {
+    return solver_mode == BFE_MODE_VEL_CURRENT ? 2.0 * pdiag[i] : (2.0 - dt * cdiag[i] / m[i]);
+  };
 
   // pack rows into the sliced ELL layout
   const int64_t n_slices = (n + bfe::kSlice - 1) / bfe::kSlice;
@@ -512,13 +519,13 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
           const int64_t j = K.idx[e];
           double v = -lscale[i] * K.val[e];
           if (j == i) {
-            v += solver_mode == BFE_MODE_VEL_CURRENT ? 2.0 * pdiag[i] : (2.0 - dt * cdiag[i] / m[i]);
+            v += diag_term(i);
             has_diag = true;
           }
           rows[r].emplace_back((uint32_t)j, v);
         }
         if (!has_diag) {
-          const double v = solver_mode == BFE_MODE_VEL_CURRENT ? 2.0 * pdiag[i] : (2.0 - dt * cdiag[i] / m[i]);
+          const double v = diag_term(i);
           rows[r].emplace_back((uint32_t)i, v);
           std::sort(rows[r].begin(), rows[r].end());
         }
@@ -645,9 +652,12 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   }
   // Group block-sparse form: DOF types coupled by K form groups; each group
   // becomes a block-sparse matrix with BS x BS blocks over the nodes that
-  // carry it (requires the difference form on every row and consecutive
-  // group rows inside each node block).
-  if (precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0) {
+  // carry it (requires consecutive group rows inside each node block). FP32:
+  // the difference form on every row, blocks of the neighbour nodes only,
+  // coefficients Lp. FP64: the direct form, the node's own block included,
+  // coefficients of B with its diagonal.
+  const bool f64 = precision == BFE_PREC_DOUBLE;
+  if (nodes_ok && (f64 || (have_nodes && direct_rows == 0))) {
     std::map<int32_t, int32_t> parent;
     for (int64_t i = 0; i < n; ++i) parent.emplace(dof_type[i], dof_type[i]);
     std::function<int32_t(int32_t)> find = [&](int32_t x) {
@@ -691,13 +701,15 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         const int bs = (int)types[gi].size();
         std::vector<int32_t> nptr(1, 0), nrow;
         std::vector<float> coef;
+        std::vector<double> coef64;
         std::vector<int64_t> nb_rows;
         for (int32_t a0 : row0s[gi]) {
           nb_rows.clear();
+          if (f64) nb_rows.push_back(a0);
           for (int k = 0; k < bs; ++k)
             for (int64_t e = K.ptr[a0 + k]; e < K.ptr[a0 + k + 1]; ++e) {
               const int64_t j = K.idx[e];
-              if (dof_node[j] == dof_node[a0]) continue;
+              if (!f64 && dof_node[j] == dof_node[a0]) continue;
               nb_rows.push_back(j - type_pos[dof_type[j]].second);
             }
           std::sort(nb_rows.begin(), nb_rows.end());
@@ -710,13 +722,15 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
               const int64_t* end = K.idx.data() + K.ptr[row + 1];
               for (int l = 0; l < bs; ++l) {
                 const int64_t* hit = std::lower_bound(beg, end, b0 + l);
-                coef.push_back(hit != end && *hit == b0 + l ? (float)(lscale[row] * K.val[hit - K.idx.data()]) : 0.0f);
+                const double kv = hit != end && *hit == b0 + l ? K.val[hit - K.idx.data()] : 0.0;
+                if (f64) coef64.push_back(-lscale[row] * kv + (row == b0 + l ? diag_term(row) : 0.0));
+                else coef.push_back(kv != 0.0 ? (float)(lscale[row] * kv) : 0.0f);
               }
             }
           }
           nptr.push_back((int32_t)nrow.size());
         }
-        if (coef.size() >= (size_t)INT32_MAX) { ok = false; break; }
+        if (std::max(coef.size(), coef64.size()) >= (size_t)INT32_MAX) { ok = false; break; }
         pl->groups.bs[gi] = bs;
         pl->groups.n_nodes[gi] = (int32_t)row0s[gi].size();
         pl->groups.blk_begin[gi] = blocks;
@@ -724,6 +738,19 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         CUDA_TRY(pl->g_row0[gi].upload(row0s[gi]));
         CUDA_TRY(pl->g_nptr[gi].upload(nptr));
         CUDA_TRY(pl->g_nrow[gi].upload(nrow));
+        std::vector<int4> rec(row0s[gi].size());
+        for (size_t a0 = 0; a0 < rec.size(); ++a0)
+          rec[a0] = make_int4(row0s[gi][a0], nptr[a0], nptr[a0 + 1] - nptr[a0], 0);
+        CUDA_TRY(pl->g_rec[gi].upload(rec));
+        pl->groups.rec[gi] = pl->g_rec[gi].p;
+        pl->groups.row0[gi] = pl->g_row0[gi].p;
+        pl->groups.nptr[gi] = pl->g_nptr[gi].p;
+        pl->groups.nrow[gi] = pl->g_nrow[gi].p;
+        if (f64) {
+          CUDA_TRY(pl->g_coef64[gi].upload(coef64));
+          pl->groups.coef64[gi] = pl->g_coef64[gi].p;
+          continue;
+        }
         CUDA_TRY(pl->g_coef[gi].upload(coef));
         std::vector<int32_t> frow;
         frow.reserve(nrow.size() * bs);
@@ -735,11 +762,6 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         for (size_t k = 0; k < coef.size(); ++k) coef2[k] = make_float2(coef[k], coef[k]);
         CUDA_TRY(pl->g_coef2[gi].upload(coef2));
         pl->groups.coef2[gi] = pl->g_coef2[gi].p;
-        std::vector<int4> rec(row0s[gi].size());
-        for (size_t a0 = 0; a0 < rec.size(); ++a0)
-          rec[a0] = make_int4(row0s[gi][a0], nptr[a0], nptr[a0 + 1] - nptr[a0], 0);
-        CUDA_TRY(pl->g_rec[gi].upload(rec));
-        pl->groups.rec[gi] = pl->g_rec[gi].p;
         // padded copy: each node's pairs start on a 16-byte boundary
         std::vector<int32_t> cofs;
         std::vector<float2> coefp;
@@ -755,14 +777,11 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         CUDA_TRY(pl->g_coefp[gi].upload(coefp));
         pl->tma.cofs[gi] = pl->g_cofs[gi].p;
         pl->tma.coefp[gi] = pl->g_coefp[gi].p;
-        pl->groups.row0[gi] = pl->g_row0[gi].p;
-        pl->groups.nptr[gi] = pl->g_nptr[gi].p;
-        pl->groups.nrow[gi] = pl->g_nrow[gi].p;
         pl->groups.coef[gi] = pl->g_coef[gi].p;
       }
       pl->groups.blk_begin[pl->groups.n_groups] = blocks;
       pl->have_groups = ok && blocks > 0;
-      if (pl->have_groups) {
+      if (pl->have_groups && !f64) {
         CUDA_TRY(pl->d_err.alloc(1));
         pl->tma.err = pl->d_err.p;
       }
@@ -1832,11 +1851,13 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   RunArrays rf;
   bfe::StepArgs af;
   if ((rc = prepare_run(pl, frc, hidx, R, n_t, n_sig, d_sig.p, d_hist.p, st, rf, af))) return rc;
-  const bool use_groups = (R % 64 == 0 || R == 16 || R == 32) && pl->have_groups && prec == BFE_PREC_SINGLE;
+  const bool use_groups = pl->have_groups && (prec == BFE_PREC_SINGLE ? (R % 64 == 0 || R == 16 || R == 32)
+                                                                       : R % 16 == 0);
   const bfe::GroupArgs* grp = use_groups ? &pl->groups : nullptr;
   // the variant the forward runs chose for this R, else the half-warp kernel
-  // (raw coefficients; 3D plans map it to the warp-per-node kernel)
-  int variant = use_groups ? 20 : 0;
+  // (FP32: raw coefficients, 3D plans map it to the warp-per-node kernel;
+  // FP64: the widest group form R allows)
+  int variant = !use_groups ? 0 : prec == BFE_PREC_SINGLE ? 20 : (R % 64 == 0 ? 1 : R % 32 == 0 ? 2 : 3);
   if (use_groups) {
     auto it = pl->variant_of_R.find(R);
     if (it != pl->variant_of_R.end()) variant = it->second;

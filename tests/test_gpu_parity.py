@@ -220,6 +220,25 @@ def test_half_warp_kernels_with_16_and_32_sources(bfe, coupled, R, variant, monk
         assert _err(hb[:, :, r], h0) <= TOL32
 
 
+@pytest.mark.parametrize("R,variant", [(64, 0), (64, 1), (64, 2), (64, 3), (32, 2), (32, 3), (16, 3)])
+def test_fp64_group_kernels(bfe, coupled, R, variant, monkeypatch):
+    """FP64 plans with node information march many sources with the FP64
+    group block-sparse kernel (direct form); variant 0 is the slice kernel."""
+    m = coupled
+    nt = 150
+    t, s = modelgen.pulse(nt, m["dt"])
+    nds = np.nonzero(m["gl"][:, 3] > 0)[0] + 1
+    srcs = [modelgen.gi_of(m["gl"], [nds[(7 * r) % nds.size]], 4) for r in range(R)]
+    hi = np.concatenate([modelgen.gi_of(m["gl"], m["mon_nds"], 4), modelgen.gi_of(m["gl"], m["mon_nds"], 2)])
+    monkeypatch.setenv("BFE_VARIANT", str(variant))
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, "double", m["gl"]) as plan:
+        hb = plan.run_batched(t, srcs, s, hi)
+        assert plan.stats()["variant"] == variant
+    for r in (0, R - 1):
+        h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
+        assert _err(hb[:, :, r], h0) <= TOL64
+
+
 @pytest.mark.parametrize("prec,tol", [("double", TOL64), ("single", TOL32)])
 def test_multi_model_plan_matches_each_model(bfe, plate, coupled, prec, tol):
     """Independent models joined block-diagonally in one plan: each model's
