@@ -352,7 +352,34 @@ def run_ours(args):
     torch.cuda.synchronize()
     ms_a = e0.elapsed_time(e1)
     value_a = R * main["K"].shape[0] * steps_per_march / (ms_a * 1e-3)
+
+    def part_roofline(plan, dofs, rhs, fsig, mon, n_part, nnz_part, p_part):
+        plan.set_timing(True)
+        hist = torch.zeros((R, n_t, mon.size), dtype=torch.float64, device="cuda")
+        march32(plan, hist, dofs, rhs, fsig, mon, R)
+        torch.cuda.synchronize()
+        st_ = plan.stats()
+        plan.set_timing(False)
+        ms_ = st_["step_ms"] / max(st_["step_launches"], 1)
+        by = algorithmic_bytes(nnz_part, n_part, R, p_part, mon.size, 4)
+        return {"n_dof": int(n_part), "step_kernel_ms": ms_, "achieved_gbs": by / ms_ / 1e6,
+                "frac_of_measured_hbm": by / ms_ / 1e6 / peak,
+                "kernel": KERNEL_NAMES.get(st_["variant"], "variant %d" % st_["variant"])}
+
+    part_a = part_roofline(plan_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, main["K"].shape[0],
+                           main["K"].nnz, max(int((frc_rhs[selm] == r).sum()) for r in range(R)))
     plan_a.close()
+    # the 32 sub-domain models alone (C2b), one multi-model plan
+    part_b = None
+    if subs:
+        plan_b, offs_b = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], m["gl"]) for m in subs], dt,
+                                              bfe_gb300.VEL_CURRENT, "single")
+        sel_b = frc_dof >= offs[1]
+        mons_b = mons[mons > offs[1]] - offs[1]
+        part_b = part_roofline(plan_b, frc_dof[sel_b] - offs[1], frc_rhs[sel_b], frc_sig[sel_b], mons_b,
+                               plan_b.n, sum(m["K"].nnz for m in subs),
+                               max(int((frc_rhs[sel_b] == r).sum()) for r in range(R)))
+        plan_b.close()
 
     # end to end through the C ABI with host buffers (H2D signals, D2H A-scans)
     e2e_steps = 1
@@ -401,7 +428,8 @@ def run_ours(args):
                            "speedup_fp32_batched": value / world / value64},
             "ascan_err_vs_fp64": err,
             "coupled_fmc_only": {"value": value_a, "unit": UNIT, "ms_per_march": ms_a,
-                                 "n_dof": int(main["K"].shape[0])},
+                                 "n_dof": int(main["K"].shape[0]), "roofline": part_a},
+            "subdomains_only": part_b,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
             "gpu_launches": launches,

@@ -904,6 +904,78 @@ __device__ __forceinline__ void group4_nbr(const float* nb, const float2* coef, 
   }
 }
 
+// Compensated update of four right-hand sides of one row (c .. c + 3):
+// u_new = u_n + q (u_n - u_{n-1}) - Lp u_n + forcing with the two-sum of
+// (u_n - u_{n-1}), interface staging and history as the other kernels.
+__device__ __forceinline__ void finish4(const StepArgs& a, int row, int c, float4 uo, float4 acc, float4 up) {
+  const uint32_t info = __ldg(a.rowinfo + row);
+  const float q = __ldg(static_cast<const float*>(a.rowc) + row);
+  const size_t o = (size_t)row * a.R + c;
+  const float2 q2 = make_float2(q, q);
+  float2 res[2], vin[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float2 u = h ? make_float2(uo.z, uo.w) : make_float2(uo.x, uo.y);
+    const float2 p = h ? make_float2(up.z, up.w) : make_float2(up.x, up.y);
+    const float2 ac = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
+    float2 d, err;
+    two_sum2(u, make_float2(-p.x, -p.y), d, err);
+    float2 inc = __ffma2_rn(q2, d, ac);                        // q d - Lp u
+    if (info & kRowForced)
+      inc = __fadd2_rn(inc, make_float2(forcing_sum<float>(a, row, c + 2 * h),
+                                        forcing_sum<float>(a, row, c + 2 * h + 1)));
+    inc = __ffma2_rn(q2, err, inc);
+    res[h] = __fadd2_rn(u, inc);
+    vin[h] = a.int_base_prev ? __fadd2_rn(__fadd2_rn(d, err), inc) : __fadd2_rn(d, err);
+  }
+  *reinterpret_cast<float4*>(static_cast<float*>(a.u_new) + o) = make_float4(res[0].x, res[0].y, res[1].x, res[1].y);
+  if (info & kRowInterface) {
+    const int t = lower_bound_i32(a.int_row, a.n_int, row);
+    *reinterpret_cast<float4*>(static_cast<float*>(a.v_int) + (size_t)t * a.R + c) =
+        make_float4(vin[0].x, vin[0].y, vin[1].x, vin[1].y);
+  } else if (info & kRowMonitored) {
+    write_history(a, row, c, (double)res[0].x);
+    write_history(a, row, c + 1, (double)res[0].y);
+    write_history(a, row, c + 2, (double)res[1].x);
+    write_history(a, row, c + 3, (double)res[1].y);
+  }
+}
+
+// One-DOF (fluid) node with 8 lanes: each lane carries the right-hand sides
+// c .. c + 3 and c + 32 .. c + 35, so a neighbour's index and coefficient
+// serve 512 bytes of state as in the two-DOF form.
+template <int UNROLL, bool RAW>
+__device__ __forceinline__ void group4_fluid(const StepArgs& a, const GroupArgs& gr, int gi, int node, int l8) {
+  const int4 rec = __ldg(gr.rec[gi] + node);
+  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
+  const int R = a.R;
+  const size_t rs = (size_t)R;
+  const float* un = static_cast<const float*>(a.u_n);
+  const int32_t* nrow = gr.nrow[gi];
+  const float2* coef = gr.coef2[gi];
+  const float* craw = gr.coef[gi];
+  for (int c = l8 * 4; c < R; c += 64) {
+    const float* own = un + (size_t)row0 * rs + c;
+    const float4 uo0 = __ldg(reinterpret_cast<const float4*>(own));
+    const float4 uo1 = __ldg(reinterpret_cast<const float4*>(own + 32));
+    float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
+#pragma unroll UNROLL
+    for (int e = p0; e < p1; ++e) {
+      const float* nb = un + (size_t)__ldg(nrow + e) * rs + c;
+      const float4 g0 = __ldg(reinterpret_cast<const float4*>(nb));
+      const float4 g1 = __ldg(reinterpret_cast<const float4*>(nb + 32));
+      float2 cv;
+      if (RAW) { const float cr = __ldg(craw + e); cv = make_float2(cr, cr); }
+      else cv = __ldg(coef + e);
+      acc0 = f4fma(cv, f4sub(uo0, g0), acc0);
+      acc1 = f4fma(cv, f4sub(uo1, g1), acc1);
+    }
+    const float* upv = static_cast<const float*>(a.u_prev) + (size_t)row0 * rs + c;
+    finish4(a, row0, c, uo0, acc0, __ldcs(reinterpret_cast<const float4*>(upv)));
+    finish4(a, row0, c + 32, uo1, acc1, __ldcs(reinterpret_cast<const float4*>(upv + 32)));
+  }
+}
+
 template <int BS, int UNROLL, bool LATE_UP, bool RAW, int LPN>
 __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& gr, int gi, int node,
                                             int l16) {
@@ -928,42 +1000,12 @@ __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& 
 #pragma unroll UNROLL
     for (int e = p0; e < p1; ++e)
       group4_nbr<BS, RAW>(un + (size_t)__ldg(nrow + e) * rs + c, coef, craw, e, rs, uo, acc);
-    float* unew = static_cast<float*>(a.u_new);
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
       const int row = row0 + k;
-      const uint32_t info = __ldg(a.rowinfo + row);
-      const float q = __ldg(static_cast<const float*>(a.rowc) + row);
-      const size_t o = (size_t)row * rs + c;
-      if (LATE_UP) up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) + o));
-      const float2 q2 = make_float2(q, q);
-      float2 res[2], vin[2];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const float2 u = h ? make_float2(uo[k].z, uo[k].w) : make_float2(uo[k].x, uo[k].y);
-        const float2 p = h ? make_float2(up[k].z, up[k].w) : make_float2(up[k].x, up[k].y);
-        const float2 ac = h ? make_float2(acc[k].z, acc[k].w) : make_float2(acc[k].x, acc[k].y);
-        float2 d, err;
-        two_sum2(u, make_float2(-p.x, -p.y), d, err);
-        float2 inc = __ffma2_rn(q2, d, ac);                    // q d - Lp u
-        if (info & kRowForced)
-          inc = __fadd2_rn(inc, make_float2(forcing_sum<float>(a, row, c + 2 * h),
-                                            forcing_sum<float>(a, row, c + 2 * h + 1)));
-        inc = __ffma2_rn(q2, err, inc);
-        res[h] = __fadd2_rn(u, inc);
-        vin[h] = a.int_base_prev ? __fadd2_rn(__fadd2_rn(d, err), inc) : __fadd2_rn(d, err);
-      }
-      *reinterpret_cast<float4*>(unew + o) = make_float4(res[0].x, res[0].y, res[1].x, res[1].y);
-      if (info & kRowInterface) {
-        const int t = lower_bound_i32(a.int_row, a.n_int, row);
-        *reinterpret_cast<float4*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) =
-            make_float4(vin[0].x, vin[0].y, vin[1].x, vin[1].y);
-      } else if (info & kRowMonitored) {
-        write_history(a, row, c, (double)res[0].x);
-        write_history(a, row, c + 1, (double)res[0].y);
-        write_history(a, row, c + 2, (double)res[1].x);
-        write_history(a, row, c + 3, (double)res[1].y);
-      }
+      if (LATE_UP)
+        up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) + (size_t)row * rs + c));
+      finish4(a, row, c, uo[k], acc[k], up[k]);
     }
   }
 }
@@ -978,6 +1020,12 @@ __global__ void __launch_bounds__(128, MINB) step_f32_group4(StepArgs a, GroupAr
 #pragma unroll
   for (int k = 1; k < kMaxGroups; ++k)
     if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
+  if (LPN == 16 && gr.bs[gi] == 1) {                    // one-DOF nodes: 8 lanes, 16 nodes per CTA
+    const int node = (b - gr.blk_begin[gi]) * 16 + (threadIdx.x >> 3);
+    if (node >= gr.n_nodes[gi]) return;
+    group4_fluid<UNROLL, RAW>(a, gr, gi, node, threadIdx.x & 7);
+    return;
+  }
   const int node = (b - gr.blk_begin[gi]) * (128 / LPN) + threadIdx.x / LPN;
   if (node >= gr.n_nodes[gi]) return;
   if (gr.bs[gi] == 1) group4_node<1, UNROLL * 2, LATE_UP, RAW, LPN>(a, gr, gi, node, threadIdx.x % LPN);
@@ -990,8 +1038,9 @@ static void launch_group4(const StepArgs& a, const GroupArgs& gr, int variant, c
   GroupArgs g = gr;
   int blocks = 0;
   for (int k = 0; k < g.n_groups; ++k) {
+    const int npc = (LPN == 16 && g.bs[k] == 1) ? 16 : 128 / LPN;     // nodes per CTA
     g.blk_begin[k] = blocks;
-    blocks += (g.n_nodes[k] + 128 / LPN - 1) / (128 / LPN);
+    blocks += (g.n_nodes[k] + npc - 1) / npc;
   }
   g.blk_begin[g.n_groups] = blocks;
   switch (variant) {
