@@ -402,7 +402,10 @@ def fn_explicit_dynamic_solver_gb300(K, C, M, time, forcing_indices, forcing_fun
     time = np.asarray(time, float).ravel()
     dt = time[1] - time[0]
     is_vel = field_output_type not in DISP_FIELD_TYPES
-    with Plan(K, C, M, dt, solver_mode, solver_precision, gl_lookup) as plan:
+    # node information serves the FP32 difference form; an FP64 plan would
+    # only use it for many-source kernels, which one load step never runs
+    single = _precision_code(solver_precision) == _lib.BFE_PREC_SINGLE
+    with Plan(K, C, M, dt, solver_mode, solver_precision, gl_lookup if single else None) as plan:
         hist, fld, fld_t = plan.run(time, forcing_indices, forcing_functions, history_indices,
                                     field_output_every_n_frames, is_vel)
     if history_indices is None or len(np.ravel(history_indices)) == 0:
@@ -429,7 +432,8 @@ def fn_explicit_dynamic_solver_v5_gb300(K, C, M, time, forcing_indices, forcing_
         raise SolverError("M must be square matrix, same size as K")          # v5.m:56-58
     time = np.asarray(time, float).ravel()
     dt = time[1] - time[0]
-    with Plan(K, C, M, dt, V5, solver_precision, gl_lookup) as plan:
+    single = _precision_code(solver_precision) == _lib.BFE_PREC_SINGLE
+    with Plan(K, C, M, dt, V5, solver_precision, gl_lookup if single else None) as plan:
         hist, fld, frc, fld_t = plan.run_v5(time, forcing_indices, forcing_functions, disp_indices,
                                             disp_functions, history_indices,
                                             field_output_every_n_frames)
