@@ -668,9 +668,34 @@ def cpu_baseline(K, C, M, dt, t, src_gi, sig, mons, target_s=10.0):
             "sample": "one source, first %d of %d samples, FP64 v6 loop (C, OpenMP)" % (steps, len(t))}
 
 
+def _ref_subdomain(args):
+    """Worker: one steel sub-domain model (square with absorbing layers on
+    every side and a seeded void blob) built with the oracle's restatements
+    of the reference's mesh and assembly code; returns (K, C, M, dt)."""
+    from oracle import assembly, mesh, signals
+    side, seed, h, fc = args
+    steel = dict(rho=8000.0, D=signals.isotropic_stiffness_matrix(210e9, 0.3), el_typ="CPE3")
+    mod = mesh.rectangular_structured_mesh(np.array([[0, 0], [side, 0], [side, side], [0, side]]), h)
+    rng = np.random.default_rng(seed)
+    blob = mesh.create_smooth_random_blob(0.5, 4, 64, rng) * (side / 10) + np.array([side / 2, side / 2])
+    mod = mesh.remove_elements_in_region(mod, blob)
+    cL = np.sqrt(steel["D"][0, 0] / steel["rho"])
+    th = 3.0 * cL / fc
+    inner = np.array([[th, th], [side - th, th], [side - th, side - th], [th, side - th]])
+    mod = mesh.add_absorbing_layer(mod, inner, th)
+    mod["el_typ_i"] = ["CPE3"] * len(mod["el_mat_i"])
+    K, C, M, _ = assembly.build_global_matrices_v5(mod["nds"], mod["els"], mod["el_mat_i"], mod["el_abs_i"],
+                                                   mod["el_typ_i"], [steel], dict(dof_to_use=[1, 2]))
+    dt = signals.element_eigen_time_step(mod["nds"], mod["els"], steel["D"], steel["rho"])
+    return K, C, M, dt
+
+
 def run_reference(args):
     """The reference's CPU path (FP64 oracle port of the v6 loop on all host
-    threads) on the same workload, each step a bounded sample."""
+    threads) on the same workload - the coupled model and the sub-domain
+    models joined into one operator, built with the oracle's restatements of
+    the reference's mesh and assembly code - each step a bounded sample of
+    one source's march."""
     rank = int(os.environ.get("RANK", 0))
     if rank != 0:
         return None
@@ -704,6 +729,24 @@ def run_reference(args):
     src = gl[mid - 1, 3]
     src = src[src > 0]
     mons = np.array([gl[top[np.argmin(np.abs(mod["nds"][top, 0] - x))], 3] for x in xc])
+    n_models = 1
+    if args.subdomains:
+        import multiprocessing as mp
+        import scipy.sparse as sp
+        from concurrent.futures import ProcessPoolExecutor
+        from bfe_gb300.model import subdomain_sides
+        sides = subdomain_sides(args.subdomains, h=w["h"]) * args.scale
+        with ProcessPoolExecutor(max_workers=min(args.subdomains, os.cpu_count() or 4),
+                                 mp_context=mp.get_context("spawn")) as ex:
+            subs = list(ex.map(_ref_subdomain, [(float(sd), 100 + k, w["h"], w["fc"])
+                                                for k, sd in enumerate(sides)]))
+        K = sp.block_diag([K] + [x[0] for x in subs], format="csr")
+        C = sp.block_diag([C] + [x[1] for x in subs], format="csr")
+        M = sp.block_diag([M] + [x[2] for x in subs], format="csr")
+        dt = min([dt] + [x[3] for x in subs])
+        t = np.arange(n_t) * dt
+        sig = signals.gaussian_pulse(t, w["fc"], w["cycles"])
+        n_models += len(subs)
     op = cpu_port.CpuOperator(K, C, M, dt)
     n = K.shape[0]
     probe = 10
@@ -723,9 +766,10 @@ def run_reference(args):
         "n_gpus": int(os.environ.get("WORLD_SIZE", 1)), "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "coupled water/steel 60x30 mm at 0.05 mm, reference CPU v6 loop "
-                               "(FP64), one source per bounded sample", "n_dof": n, "samples": n_t,
-                   "sample_steps": steps, "scale": args.scale},
+        "config": {"workload": "coupled water/steel 60x30 mm at 0.05 mm plus %d steel scatterer "
+                               "sub-domain models joined in one operator, reference CPU v6 loop (FP64), "
+                               "one source per bounded sample" % (n_models - 1),
+                   "n_dof": n, "models": n_models, "samples": n_t, "sample_steps": steps, "scale": args.scale},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_port.threads(), "kind": "port",
                          "sample": "first %d of %d samples of one source" % (steps, n_t)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
