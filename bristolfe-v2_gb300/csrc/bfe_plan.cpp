@@ -482,15 +482,18 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   bool nodes_ok = dof_node && dof_type;
   if (nodes_ok) {
     int64_t i = 0;
-    std::map<int64_t, int64_t> seen;
+    std::vector<int64_t> block_nodes;
     while (i < n && nodes_ok) {
       int64_t j = i;
       while (j < n && dof_node[j] == dof_node[i]) ++j;
-      if (j - i > 8 || seen.count(dof_node[i])) { nodes_ok = false; break; }
-      seen[dof_node[i]] = i;
+      if (j - i > 8) { nodes_ok = false; break; }
+      block_nodes.push_back(dof_node[i]);
       for (int64_t k = i; k < j; ++k) { blk_base[k] = i; blk_len[k] = j - i; }
       i = j;
     }
+    // every node's rows must be one consecutive block
+    std::sort(block_nodes.begin(), block_nodes.end());
+    if (std::adjacent_find(block_nodes.begin(), block_nodes.end()) != block_nodes.end()) nodes_ok = false;
   }
   const bool have_nodes = precision == BFE_PREC_SINGLE && nodes_ok;
   // diagonal term of B in the FP64 form (v6.m:131-138 with the diagonal of P)
@@ -658,30 +661,50 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   // coefficients of B with its diagonal.
   const bool f64 = precision == BFE_PREC_DOUBLE;
   if (nodes_ok && (f64 || (have_nodes && direct_rows == 0))) {
-    std::map<int32_t, int32_t> parent;
-    for (int64_t i = 0; i < n; ++i) parent.emplace(dof_type[i], dof_type[i]);
-    std::function<int32_t(int32_t)> find = [&](int32_t x) {
+    // DOF types as dense ids (sorted), the types K couples, their groups
+    std::vector<int32_t> type_list(dof_type, dof_type + n);
+    std::sort(type_list.begin(), type_list.end());
+    type_list.erase(std::unique(type_list.begin(), type_list.end()), type_list.end());
+    const int nt_ = (int)type_list.size();
+    bool ok = nt_ <= 3 * bfe::kMaxGroups;
+    std::vector<uint8_t> tid(n, 0);
+    if (ok)
+      for (int64_t i = 0; i < n; ++i)
+        tid[i] = (uint8_t)(std::lower_bound(type_list.begin(), type_list.end(), dof_type[i]) - type_list.begin());
+    std::vector<int> parent(std::max(nt_, 1));
+    for (int t = 0; t < nt_; ++t) parent[t] = t;
+    auto find = [&](int x) {
       while (parent[x] != x) x = parent[x] = parent[parent[x]];
       return x;
     };
-    for (int64_t i = 0; i < n; ++i)
-      for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
-        const int32_t a1 = find(dof_type[i]), b1 = find(dof_type[K.idx[e]]);
-        if (a1 != b1) parent[std::max(a1, b1)] = std::min(a1, b1);
-      }
-    std::map<int32_t, std::vector<int32_t>> gtypes;   // root -> sorted types
-    for (auto& kv : parent) gtypes[find(kv.first)].push_back(kv.first);
-    bool ok = gtypes.size() <= (size_t)bfe::kMaxGroups;
+    if (ok) {
+      std::vector<char> coupled((size_t)nt_ * nt_, 0);
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) coupled[(size_t)tid[i] * nt_ + tid[K.idx[e]]] = 1;
+      for (int a1 = 0; a1 < nt_; ++a1)
+        for (int b1 = 0; b1 < nt_; ++b1)
+          if (coupled[(size_t)a1 * nt_ + b1]) {
+            const int ra = find(a1), rb = find(b1);
+            if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
+          }
+    }
+    std::map<int, std::vector<int32_t>> gtypes;         // root -> sorted types
+    for (int t = 0; t < nt_ && ok; ++t) gtypes[find(t)].push_back(type_list[t]);
+    ok = ok && gtypes.size() <= (size_t)bfe::kMaxGroups;
     std::vector<std::vector<int32_t>> types;
     for (auto& kv : gtypes) { types.push_back(kv.second); if (kv.second.size() > 3) ok = false; }
-    std::map<int32_t, std::pair<int, int>> type_pos;  // type -> (group, position)
+    std::vector<std::pair<int, int>> tpos(std::max(nt_, 1));   // dense type -> (group, position)
     for (size_t gi = 0; gi < types.size(); ++gi)
-      for (size_t k = 0; k < types[gi].size(); ++k) type_pos[types[gi][k]] = {(int)gi, (int)k};
+      for (size_t k = 0; k < types[gi].size(); ++k) {
+        const int t = (int)(std::lower_bound(type_list.begin(), type_list.end(), types[gi][k]) - type_list.begin());
+        tpos[t] = {(int)gi, (int)k};
+      }
+    auto type_pos_of = [&](int64_t dof) { return tpos[tid[dof]]; };
     std::vector<std::vector<int32_t>> row0s(types.size());
     // every node block: each group it touches must be complete and consecutive
     for (int64_t b = 0; b < n && ok; b += blk_len[b]) {
       for (int64_t k = b; k < b + blk_len[b]; ++k) {
-        const auto tp = type_pos[dof_type[k]];
+        const auto tp = type_pos_of(k);
         if (tp.second != 0) continue;
         const auto& ty = types[tp.first];
         if (k + (int64_t)ty.size() > b + blk_len[b]) { ok = false; break; }
@@ -690,7 +713,7 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
         row0s[tp.first].push_back((int32_t)k);
       }
       for (int64_t k = b; k < b + blk_len[b]; ++k) {
-        const auto tp = type_pos[dof_type[k]];
+        const auto tp = type_pos_of(k);
         if (tp.second != 0 && (k - tp.second < b || dof_type[k - tp.second] != types[tp.first][0])) ok = false;
       }
     }
@@ -710,7 +733,7 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
             for (int64_t e = K.ptr[a0 + k]; e < K.ptr[a0 + k + 1]; ++e) {
               const int64_t j = K.idx[e];
               if (!f64 && dof_node[j] == dof_node[a0]) continue;
-              nb_rows.push_back(j - type_pos[dof_type[j]].second);
+              nb_rows.push_back(j - type_pos_of(j).second);
             }
           std::sort(nb_rows.begin(), nb_rows.end());
           nb_rows.erase(std::unique(nb_rows.begin(), nb_rows.end()), nb_rows.end());
