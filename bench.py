@@ -400,8 +400,14 @@ def run_ours(args):
         extra["adjoint_c4"] = adjoint_section(torch, bfe_gb300, model)
     result = None
     if rank == 0:
-        cpu = cpu_baseline(main["K"], main["C"], main["M"], dt, t, srcs[r_mid][srcs[r_mid] <= offs[1]],
-                           sig, mons_a) if world == 1 else None
+        cpu = None
+        if world == 1:
+            import scipy.sparse as sp
+            Kj = sp.block_diag([m["K"] for m in models], format="csr")
+            Cj = sp.block_diag([m["C"] for m in models], format="csr")
+            Mj = sp.block_diag([m["M"] for m in models], format="csr")
+            cpu = cpu_baseline(Kj, Cj, Mj, dt, t, srcs[r_mid], sig, mons)
+            cpu["sample"] += ", all %d models joined in one operator" % len(models)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
