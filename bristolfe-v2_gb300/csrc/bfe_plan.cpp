@@ -62,6 +62,45 @@ int to_csr(const bfe_sparse* A, const char* name, Csr& out) {
   const int64_t nmaj = csc ? A->n_cols : A->n_rows;
   const int64_t nmin = csc ? A->n_rows : A->n_cols;
   if (A->ptr && (A->ptr[0] != 0 || A->ptr[nmaj] != A->nnz)) return fail(BFE_ERR_ARG, "%s: bad pointer array", name);
+  if (!A->ptr) {                                   // an empty matrix may come without arrays
+    if (nmaj > 0 && A->nnz > 0) return fail(BFE_ERR_ARG, "%s has NULL arrays", name);
+    out.n = A->n_rows;
+    out.m = A->n_cols;
+    out.ptr.assign(out.n + 1, 0);
+    out.idx.clear();
+    out.val.clear();
+    return BFE_OK;
+  }
+  if (!csc) {
+    // CSR input whose rows are strictly increasing (SciPy after
+    // sum_duplicates, the joined multi-model matrices): validate and copy,
+    // dropping exact zeros; anything else takes the general path below
+    bool fast = true;
+    for (int64_t a = 0; a < nmaj && fast; ++a) {
+      if (A->ptr[a + 1] < A->ptr[a]) return fail(BFE_ERR_ARG, "%s: pointer array not monotone", name);
+      for (int64_t e = A->ptr[a]; e < A->ptr[a + 1]; ++e) {
+        const int64_t b = A->idx[e];
+        if (b < 0 || b >= nmin) return fail(BFE_ERR_ARG, "%s: index %lld out of range", name, (long long)b);
+        if (!std::isfinite(A->val[e])) return fail(BFE_ERR_NUMERIC, "%s has a non-finite value", name);
+        if (e > A->ptr[a] && b <= A->idx[e - 1]) { fast = false; break; }
+      }
+    }
+    if (fast) {
+      out.n = A->n_rows;
+      out.m = A->n_cols;
+      out.ptr.assign(out.n + 1, 0);
+      out.idx.clear();
+      out.val.clear();
+      out.idx.reserve(A->nnz);
+      out.val.reserve(A->nnz);
+      for (int64_t a = 0; a < nmaj; ++a) {
+        for (int64_t e = A->ptr[a]; e < A->ptr[a + 1]; ++e)
+          if (A->val[e] != 0.0) { out.idx.push_back(A->idx[e]); out.val.push_back(A->val[e]); }
+        out.ptr[a + 1] = (int64_t)out.idx.size();
+      }
+      return BFE_OK;
+    }
+  }
   std::vector<int64_t> rows, cols;
   rows.reserve(A->nnz);
   cols.reserve(A->nnz);
