@@ -238,17 +238,26 @@ struct GradArgs {
   const void* ke;             // n_el x ndf x ndf unit-scale stiffness (plan precision)
   const void* mh;             // n_el x ndf lumped mass per unit density
   const void* ch;             // n_el x ndf damping per unit density
-  const void* lam;            // lam_t   [n][R]
-  const void* u0;             // u_t     [n][R]
-  const void* u1;             // u_{t-1} [n][R]
-  const void* u2;             // u_{t-2} [n][R]
+  // n_steps consecutive steps t_k = t_0 + k: lam_{t_k} in slot k of `lam`,
+  // u_{t_k - 2}, u_{t_k - 1}, u_{t_k} in slots k, k + 1, k + 2 of `u`; each
+  // slot is an [n][R] array, `stride` values after the previous one
+  const void* lam;
+  const void* u;
+  int64_t stride;
+  int n_steps;
   int R;
+  int64_t n;                  // rows of a state slot
   double dt;
   double* gs;                 // dJ/ds   accumulators (n_el)
   double* gr;                 // dJ/drho accumulators (n_el)
+  double* pw;                 // per-DOF sums of lam_t (u_t - 2 u_{t-1} + u_{t-2}) (n)
+  double* pv;                 // per-DOF sums of lam_t (u_t - u_{t-2}) (n)
 };
 bool grad_ndf_supported(int ndf);
+// one segment: gs and the per-DOF sums pw, pv
 cudaError_t launch_grad(const GradArgs& g, int precision, cudaStream_t s);
+// after the last segment: gr from pw, pv
+cudaError_t launch_grad_rho(const GradArgs& g, int precision, cudaStream_t s);
 
 // Message returned by bfe_last_error() on the calling thread.
 void set_last_error(const char* msg);

@@ -337,6 +337,19 @@ void push_val(std::vector<unsigned char>& buf, double v) {
   buf.insert(buf.end(), b, b + sizeof(T));
 }
 
+// count doubles converted to T, as bytes
+template <typename T>
+std::vector<unsigned char> cast_bytes(const double* v, int64_t count) {
+  std::vector<T> x(v, v + count);
+  std::vector<unsigned char> b((size_t)count * sizeof(T));
+  if (count) std::memcpy(b.data(), x.data(), b.size());
+  return b;
+}
+
+std::vector<unsigned char> cast_bytes(int prec, const double* v, int64_t count) {
+  return prec == BFE_PREC_DOUBLE ? cast_bytes<double>(v, count) : cast_bytes<float>(v, count);
+}
+
 int upload_bytes(DevBuf<unsigned char>& d, const std::vector<unsigned char>& h) {
   CUDA_TRY(d.upload(h));
   return BFE_OK;
@@ -1884,16 +1897,9 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   {
     std::vector<int32_t> hd(el_dof, el_dof + n_el * ndf);
     CUDA_TRY(d_dof.upload(hd));
-    std::vector<unsigned char> b1, b2, b3;
-    for (int64_t k = 0; k < n_el * ndf * ndf; ++k)
-      prec == BFE_PREC_DOUBLE ? push_val<double>(b1, ke[k]) : push_val<float>(b1, ke[k]);
-    for (int64_t k = 0; k < n_el * ndf; ++k) {
-      prec == BFE_PREC_DOUBLE ? push_val<double>(b2, mh[k]) : push_val<float>(b2, mh[k]);
-      prec == BFE_PREC_DOUBLE ? push_val<double>(b3, ch[k]) : push_val<float>(b3, ch[k]);
-    }
-    CUDA_TRY(d_ke.upload(b1));
-    CUDA_TRY(d_mh.upload(b2));
-    CUDA_TRY(d_ch.upload(b3));
+    CUDA_TRY(d_ke.upload(cast_bytes(prec, ke, n_el * ndf * ndf)));
+    CUDA_TRY(d_mh.upload(cast_bytes(prec, mh, n_el * ndf)));
+    CUDA_TRY(d_ch.upload(cast_bytes(prec, ch, n_el * ndf)));
   }
   // forward inputs
   const int64_t n_sig = frc_rows * R;
@@ -1983,19 +1989,24 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   bfe::StepArgs aa;
   std::vector<int64_t> no_mon;
   if ((rc = prepare_run(pl, afrc, no_mon, R, n_t, n_rsig, d_res.p, nullptr, st, ra, aa))) return rc;
-  // backward sweep
+  // backward sweep: a segment's forward states u_{t-2} .. u_{te-1} and
+  // adjoint states lam_t .. lam_{te+1} sit in slots t - ts of d_seg / d_lam
   DevBuf<unsigned char> d_seg, d_lam;
   DevBuf<double> d_gs, d_gr;
   CUDA_TRY(d_seg.alloc((size_t)(c + 2) * sb));
-  CUDA_TRY(d_lam.alloc(3 * sb));
-  CUDA_TRY(cudaMemsetAsync(d_lam.p, 0, 3 * sb, st));
+  CUDA_TRY(d_lam.alloc((size_t)(c + 2) * sb));
+  CUDA_TRY(cudaMemsetAsync(d_lam.p, 0, (size_t)(c + 2) * sb, st));
   CUDA_TRY(d_gs.alloc(n_el));
   CUDA_TRY(d_gr.alloc(n_el));
   CUDA_TRY(cudaMemsetAsync(d_gs.p, 0, n_el * sizeof(double), st));
   CUDA_TRY(cudaMemsetAsync(d_gr.p, 0, n_el * sizeof(double), st));
-  unsigned char* L[3] = {d_lam.p, d_lam.p + sb, d_lam.p + 2 * sb};
-  int lp = 0, lc = 1, lw = 2;        // lam_{t+2}, lam_{t+1}, lam_t
+  DevBuf<double> d_pw, d_pv;
+  CUDA_TRY(d_pw.alloc(n));
+  CUDA_TRY(d_pv.alloc(n));
+  CUDA_TRY(cudaMemsetAsync(d_pw.p, 0, n * sizeof(double), st));
+  CUDA_TRY(cudaMemsetAsync(d_pv.p, 0, n * sizeof(double), st));
   auto S = [&](int64_t k) { return d_seg.p + (size_t)k * sb; };
+  auto Lm = [&](int64_t k) { return d_lam.p + (size_t)k * sb; };
   af.n_mon = 0;                      // the recompute does not rewrite the history
   bfe::GradArgs g{};
   g.n_el = n_el;
@@ -2008,6 +2019,12 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   g.dt = dt;
   g.gs = d_gs.p;
   g.gr = d_gr.p;
+  g.lam = d_lam.p;
+  g.u = d_seg.p;
+  g.stride = n * R;
+  g.n = n;
+  g.pw = d_pw.p;
+  g.pv = d_pv.p;
   for (int64_t j = n_seg - 1; j >= 0; --j) {
     const int64_t ts = ti0 + j * c, te = std::min(ts + c, n_t);
     CUDA_TRY(cudaMemcpyAsync(S(0), d_ck.p + 2 * sb * j, 2 * sb, cudaMemcpyDeviceToDevice, st));
@@ -2020,18 +2037,24 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
     }
     for (int64_t t = te - 1; t >= ts; --t) {
       aa.ti = t;
-      aa.u_prev = L[lp];
-      aa.u_n = L[lc];
-      aa.u_new = L[lw];
+      aa.u_prev = Lm(t - ts + 2);
+      aa.u_n = Lm(t - ts + 1);
+      aa.u_new = Lm(t - ts);
       if ((rc = step(aa))) return rc;
-      g.lam = L[lw];
-      g.u0 = S(t - ts + 2);
-      g.u1 = S(t - ts + 1);
-      g.u2 = S(t - ts);
-      const cudaError_t e = bfe::launch_grad(g, prec, st);
-      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "gradient kernel launch failed: %s", cudaGetErrorString(e));
-      const int tt = lp; lp = lc; lc = lw; lw = tt;
     }
+    g.n_steps = (int)(te - ts);
+    const cudaError_t e = bfe::launch_grad(g, prec, st);
+    if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "gradient kernel launch failed: %s", cudaGetErrorString(e));
+    if (j > 0) {
+      // lam_ts, lam_{ts+1} start the previous segment (slots c, c + 1);
+      // slot 1 moves first so that c = 1 never overwrites an unread slot
+      CUDA_TRY(cudaMemcpyAsync(Lm(c + 1), Lm(1), sb, cudaMemcpyDeviceToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(Lm(c), Lm(0), sb, cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  {
+    const cudaError_t e = bfe::launch_grad_rho(g, prec, st);
+    if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "gradient kernel launch failed: %s", cudaGetErrorString(e));
   }
   CUDA_TRY(cudaMemcpyAsync(g_stiff, d_gs.p, n_el * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaMemcpyAsync(g_rho, d_gr.p, n_el * sizeof(double), cudaMemcpyDeviceToHost, st));
