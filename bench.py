@@ -50,6 +50,9 @@ def parse():
                     help="skip the 3D and adjoint sections (quick runs)")
     ap.add_argument("--subdomains", type=int, default=32,
                     help="steel sub-domain models marched with the coupled model (32 = benchmark)")
+    ap.add_argument("--only", choices=["adjoint"], default=None,
+                    help="run one extra section alone and print its JSON (profiling); --n-t sets its "
+                         "samples, finite-difference checks are skipped")
     return ap.parse_args()
 
 
@@ -585,7 +588,7 @@ def hex3d_section(torch, bfe_gb300, model):
     return out
 
 
-def adjoint_section(torch, bfe_gb300, model, n_fd=20):
+def adjoint_section(torch, bfe_gb300, model, n_fd=20, n_t=4000):
     """Adjoint gradient on the 30 x 15 mm steel plate at 0.05 mm (~360k
     triangles): 16 sources x 16 receivers, 4,000 samples, observed A-scans
     from a seeded +-5 % stiffness perturbation (1 mm Gaussian bumps),
@@ -595,7 +598,6 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20):
     m = model.steel_plate_adjoint()
     ke, mh, ch, dof = m["element_data"]
     n = m["K"].shape[0]
-    n_t = 4000
     dt = m["dt"]
     t = np.arange(n_t) * dt
     sig = model.toneburst(t, 5e6, 5)
@@ -622,6 +624,8 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20):
     _, gs32, gr32 = grads["single"]
     res["fp32_vs_fp64_rel"] = {"stiffness": float(np.linalg.norm(gs32 - gs64) / np.linalg.norm(gs64)),
                                "density": float(np.linalg.norm(gr32 - gr64) / np.linalg.norm(gr64))}
+    if n_fd < 1:
+        return res
     rng = np.random.default_rng(3)
     sens = np.nonzero(np.abs(gs64) >= 1e-2 * np.abs(gs64).max())[0]
     picks = rng.choice(sens, min(n_fd, sens.size), replace=False)
@@ -784,9 +788,22 @@ def run_reference(args):
     return line
 
 
+def run_only(args):
+    """One extra section alone on cuda:0 (profiling runs)."""
+    import torch
+    import bfe_gb300
+    from bfe_gb300 import model
+    torch.cuda.set_device(0)
+    bfe_gb300.load()
+    res = adjoint_section(torch, bfe_gb300, model, n_fd=0, n_t=args.n_t or 4000)
+    print(json.dumps({"section": "adjoint_c4", **res}), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.only:
+        run_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -357,7 +357,8 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
  * (0 = ceil(sqrt(steps))), the backward sweep recomputes each segment from
  * its checkpoint, steps the adjoint through it and contracts the segment
  * into the gradients in one pass. Device memory: about 2 n R (steps / c
- * + 2 c) values for c = ckpt_every. Only 'vel at curent time step' plans.
+ * + c) state values for c = ckpt_every (checkpoints, and the segment's
+ * forward and adjoint states). Only 'vel at curent time step' plans.
  * hist_out (optional) receives the forward A-scans.
  */
 int bfe_adjoint_gradient(bfe_plan* plan, int64_t n_el, int32_t ndf, const int64_t* el_dof,
