@@ -216,3 +216,84 @@ def test_brick_adjoint_matches_oracle(bfe, prec, tol):
     assert abs(J1 - J0) <= tol * J0
     assert np.abs(gs1 - gs0).max() <= tol * np.abs(gs0).max()
     assert np.abs(gr1 - gr0).max() <= tol * np.abs(gr0).max()
+
+
+@pytest.mark.parametrize("prec,R,tol", [("double", 2, 1e-8), ("double", 16, 1e-8), ("single", 16, 1e-3)])
+def test_three_dof_cpe3_adjoint_matches_oracle(bfe, prec, R, tol):
+    """CPE3 with DOFs 1, 2 and 3 (9 DOFs per element, out-of-plane motion
+    included) and an absorbing layer: gradients against the oracle."""
+    m = modelgen.solid_plate(W=2e-3, H=1e-3, h=0.1e-3, dof_to_use=(1, 2, 3), abs_thick=0.3e-3)
+    mod = m["mod"]
+    rho = 8000.0
+    ke, mh, ch, dof = model.cpe3_element_data(mod["nds"], mod["els"], mod["el_abs_i"], modelgen.STEEL["D"], rho,
+                                              m["gl"], dof_to_use=(1, 2, 3))
+    assert dof.shape[1] == 9
+    n = m["K"].shape[0]
+    nt = 250
+    t = np.arange(nt) * m["dt"]
+    sig = signals.gaussian_pulse(t, 5e6, 5)
+    top = m["mon_nds"]
+    srcs = [modelgen.gi_of(m["gl"], [top[(5 * k) % top.size]], 1 + k % 3) for k in range(R)]
+    hi = np.concatenate([modelgen.gi_of(m["gl"], top, 2), modelgen.gi_of(m["gl"], top, 3)])
+    rho_e = np.full(len(dof), rho)
+    rng = np.random.default_rng(11)
+    s_true = 1 + 0.05 * np.tanh(rng.standard_normal(len(dof)))
+    Kt, Ct, Mt = model.assemble_from_elements(ke, mh, ch, dof, n, s_true, rho_e)
+    obs = np.zeros((hi.size, nt, R))
+    for r, fi in enumerate(srcs):
+        obs[:, :, r] = oadj.forward(Kt, Mt.diagonal(), Ct.diagonal(), m["dt"], nt, fi - 1, sig[None, :], 0)[hi - 1]
+    J0, gs0, gr0 = oadj.misfit_and_gradient(ke, mh, ch, dof, n, m["dt"], nt, [s - 1 for s in srcs], sig[None, :],
+                                            hi - 1, obs, rho_e=rho_e)
+    K, C, M = model.assemble_from_elements(ke, mh, ch, dof, n, None, rho_e)
+    with bfe.Plan(K, C, M, m["dt"], bfe.VEL_CURRENT, prec, m["gl"]) as plan:
+        J1, gs1, gr1 = plan.adjoint_gradient((ke, mh, ch, dof), t, srcs, sig, hi, obs)
+    assert abs(J1 - J0) <= tol * J0
+    assert np.abs(gs1 - gs0).max() <= tol * np.abs(gs0).max()
+    assert np.abs(gr1 - gr0).max() <= tol * np.abs(gr0).max()
+
+
+@pytest.mark.parametrize("prec,R,tol", [("double", 4, 1e-8), ("single", 16, 1e-3)])
+def test_one_dof_triangle_adjoint_matches_oracle(bfe, prec, R, tol):
+    """Scalar waves on linear triangles (one DOF per node, 3 per element, the
+    fluid element's layout), bulk modulus 2.2 GPa, density 1000, damped
+    absorber elements: gradients against the oracle."""
+    m = modelgen.solid_plate(W=2e-3, H=1e-3, h=0.1e-3, abs_thick=0.3e-3)
+    mod = m["mod"]
+    nds, els = mod["nds"], mod["els"][:, :3] - 1
+    x, y = nds[els, 0], nds[els, 1]
+    det = (x[:, 1] - x[:, 0]) * (y[:, 2] - y[:, 0]) - (x[:, 2] - x[:, 0]) * (y[:, 1] - y[:, 0])
+    area = 0.5 * np.abs(det)
+    b = np.stack([y[:, 1] - y[:, 2], y[:, 2] - y[:, 0], y[:, 0] - y[:, 1]], 1) / det[:, None]
+    c = np.stack([x[:, 2] - x[:, 1], x[:, 0] - x[:, 2], x[:, 1] - x[:, 0]], 1) / det[:, None]
+    a = np.asarray(mod["el_abs_i"], float)
+    ke = 2.2e9 * area[:, None, None] * (b[:, :, None] * b[:, None, :] + c[:, :, None] * c[:, None, :])
+    ke *= np.exp(np.log(0.01) * a ** 4)[:, None, None]
+    mh = np.repeat(area[:, None] / 3, 3, axis=1)
+    ch = mh * (a ** 3 * 3.1415e7)[:, None]
+    dof = els.astype(np.int64)
+    n = nds.shape[0]
+    rho = 1000.0
+    lam = max(np.linalg.eigvalsh(ke[e] / (rho * mh[e][:, None])).max() for e in range(0, len(dof), 7))
+    dt = 0.8 * 2.0 / np.sqrt(lam)
+    nt = 250
+    t = np.arange(nt) * dt
+    sig = signals.gaussian_pulse(t, 2e6, 5)
+    top = m["mon_nds"] - 1
+    srcs = [np.array([top[(3 * k) % top.size] + 1]) for k in range(R)]
+    hi = top[::2] + 1
+    rho_e = np.full(len(dof), rho)
+    rng = np.random.default_rng(13)
+    s_true = 1 + 0.05 * np.tanh(rng.standard_normal(len(dof)))
+    Kt, Ct, Mt = model.assemble_from_elements(ke, mh, ch, dof, n, s_true, rho_e)
+    obs = np.zeros((hi.size, nt, R))
+    for r, fi in enumerate(srcs):
+        obs[:, :, r] = oadj.forward(Kt, Mt.diagonal(), Ct.diagonal(), dt, nt, fi - 1, sig[None, :], 0)[hi - 1]
+    J0, gs0, gr0 = oadj.misfit_and_gradient(ke, mh, ch, dof, n, dt, nt, [s - 1 for s in srcs], sig[None, :],
+                                            hi - 1, obs, rho_e=rho_e)
+    assert J0 > 0 and np.abs(gs0).max() > 0
+    K, C, M = model.assemble_from_elements(ke, mh, ch, dof, n, None, rho_e)
+    with bfe.Plan(K, C, M, dt, bfe.VEL_CURRENT, prec) as plan:
+        J1, gs1, gr1 = plan.adjoint_gradient((ke, mh, ch, dof), t, srcs, sig, hi, obs)
+    assert abs(J1 - J0) <= tol * J0
+    assert np.abs(gs1 - gs0).max() <= tol * np.abs(gs0).max()
+    assert np.abs(gr1 - gr0).max() <= tol * np.abs(gr0).max()
