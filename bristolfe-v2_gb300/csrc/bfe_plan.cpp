@@ -1847,9 +1847,12 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
 // include/bfe_gb300.h). Forward march with checkpoints of (u_{t-2}, u_{t-1})
 // every c steps and the monitored history; residuals and misfit on the host
 // in FP64; backward sweep over segments: recompute the segment's states from
-// its checkpoint, then step the adjoint (the same operator, driven by the
-// residuals) backwards through the segment and contract each step into the
-// per-element gradient accumulators.
+// its checkpoint into consecutive slots, step the adjoint (the same
+// operator, driven by the residuals) backwards through the segment into
+// slots of its own, then contract the whole segment into the per-element
+// stiffness accumulators and per-DOF density sums with one launch pair
+// (bfe_adjoint.cu); the density sums become per-element gradients once,
+// after the last segment.
 int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t* el_dof,
                          const double* ke, const double* mh, const double* ch,
                          int64_t R, int64_t n_t, const double* time,

@@ -157,16 +157,18 @@ def test_fp32_adjoint_with_16_sources_matches_fp64(bfe, problem):
     assert np.linalg.norm(gr32 - gr64) <= 1e-4 * np.linalg.norm(gr64)
 
 
-def test_fp64_adjoint_with_16_sources_matches_oracle(bfe, problem):
+@pytest.mark.parametrize("R", [1, 16])
+def test_fp64_adjoint_with_1_or_16_sources_matches_oracle(bfe, problem, R):
     """16 sources: the FP64 contraction reads two sources per 16-byte load
     with eight lanes per element; every source's gradient adds up as the
-    oracle's per-source sum."""
+    oracle's per-source sum. One source: the one-source march kernels and a
+    lane per element."""
     P = problem
     ke, mh, ch, dof = P["ed"]
     top = P["m"]["mon_nds"]
-    srcs = [modelgen.gi_of(P["m"]["gl"], [top[k % top.size]], 1 + (k // top.size) % 2) for k in range(16)]
+    srcs = [modelgen.gi_of(P["m"]["gl"], [top[k % top.size]], 1 + (k // top.size) % 2) for k in range(R)]
     rng = np.random.default_rng(5)
-    obs = 1e-3 * rng.standard_normal((P["hi1"].size, P["t"].size, 16)) * np.abs(P["obs"]).max()
+    obs = 1e-3 * rng.standard_normal((P["hi1"].size, P["t"].size, R)) * np.abs(P["obs"]).max()
     J0, gs0, gr0 = oadj.misfit_and_gradient(ke, mh, ch, dof, P["n"], P["dt"], P["t"].size,
                                             [s - 1 for s in srcs], P["sig"][None, :], P["hi1"] - 1, obs,
                                             rho_e=P["rho_e"])
@@ -252,7 +254,7 @@ def test_three_dof_cpe3_adjoint_matches_oracle(bfe, prec, R, tol):
     assert np.abs(gr1 - gr0).max() <= tol * np.abs(gr0).max()
 
 
-@pytest.mark.parametrize("prec,R,tol", [("double", 4, 1e-8), ("single", 16, 1e-3)])
+@pytest.mark.parametrize("prec,R,tol", [("double", 4, 1e-8), ("single", 16, 1e-3), ("single", 1, 1e-3)])
 def test_one_dof_triangle_adjoint_matches_oracle(bfe, prec, R, tol):
     """Scalar waves on linear triangles (one DOF per node, 3 per element, the
     fluid element's layout), bulk modulus 2.2 GPa, density 1000, damped
