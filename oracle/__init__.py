@@ -3,8 +3,8 @@
 TEST INFRASTRUCTURE ONLY. Nothing in the product package imports this
 directory; only ``tests/``, ``__graft_entry__.smoke()`` and the
 ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may use it, and
-there only as the checker or the timed CPU baseline, never as the thing
-measured or shipped.
+there only to check results or as the timed CPU baseline, never as the
+thing measured or shipped.
 
 The reference (ndtatbristol/BristolFE-v2) is a pure MATLAB toolbox and no
 MATLAB or GNU Octave exists on either machine, so the reference cannot be run.

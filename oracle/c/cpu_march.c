@@ -1,6 +1,6 @@
 /*
- * FP64 CPU restatement of the v6 time loop (TEST INFRASTRUCTURE / CPU
- * BASELINE ONLY - never linked into the product library).
+ * FP64 CPU restatement of the v6 time loop (TEST INFRASTRUCTURE AND CPU
+ * TIMING ONLY - never linked into the product library).
  *
  * Follows code/internal/fn_explicit_dynamic_solver_v6.m:180-218:
  *   f(forcing) = forcing_functions(:, ti)          (:182)

@@ -14,7 +14,7 @@ reference's own numbers for those inputs and are stored in
 independently derived element routines against them.
 
 Run in a checkout that has the reference at REFERENCE_ROOT (default
-``/root/reference``); the GPU machine never runs this script.
+``/root/reference``); the tests read only the stored fixture.
 """
 import os
 import re
