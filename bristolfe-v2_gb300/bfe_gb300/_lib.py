@@ -33,6 +33,7 @@ BFE_FIELD_DIV = 2
 BFE_FIELD_CURL = 3
 BFE_PREC_DOUBLE = 0
 BFE_PREC_SINGLE = 1
+BFE_PLAN_ONE_SOURCE = 1
 
 I64 = ctypes.c_int64
 I32 = ctypes.c_int32
@@ -72,6 +73,9 @@ SIGNATURES = {
     "bfe_plan_create": (I32, [ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
                               ctypes.POINTER(BfeSparse), ctypes.c_double, I32, I32,
                               PI64, PI32, ctypes.POINTER(VP)]),
+    "bfe_plan_create_ex": (I32, [ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
+                                 ctypes.POINTER(BfeSparse), ctypes.c_double, I32, I32,
+                                 PI64, PI32, ctypes.c_uint32, ctypes.POINTER(VP)]),
     "bfe_plan_create_multi": (I32, [I32, ctypes.POINTER(BfeSparse), ctypes.POINTER(BfeSparse),
                                     ctypes.POINTER(BfeSparse), ctypes.c_double, I32, I32,
                                     ctypes.POINTER(PI64), ctypes.POINTER(PI32), PI64,

@@ -181,6 +181,9 @@ def fn_BristolFE_v2_gb300(mod, matls, steps, fe_options=None):
     frames = not np.isinf(every)
     fcode = field_type_code(ftype)
     plans = []
+    # without step batching (or with one step) every run has one source, so
+    # the plan skips the operator forms of batched runs
+    one_source = not opt["batch_steps"] or sum(j is not None for j in jobs) == 1
 
     def plan_for(t):
         # one resident plan per time step size (steps normally share it)
@@ -188,7 +191,7 @@ def fn_BristolFE_v2_gb300(mod, matls, steps, fe_options=None):
         for p in plans:
             if abs(p.dt - dt) <= 1e-12 * abs(dt):
                 return p
-        plans.append(Plan(K, C, M, dt, mode, precision, gl))
+        plans.append(Plan(K, C, M, dt, mode, precision, gl, one_source=one_source))
         return plans[-1]
 
     field = FieldOutput(mod["nds"], mod["els"], gl, M, ftype) if frames and fcode is not None else None

@@ -77,7 +77,9 @@ class Plan:
     """Device-resident time-stepping operator (one bfe_plan)."""
 
     def __init__(self, K, C, M, dt, solver_mode=VEL_CURRENT, solver_precision="double",
-                 gl_lookup=None):
+                 gl_lookup=None, one_source=False):
+        """one_source: the plan serves one source per run (BFE_PLAN_ONE_SOURCE),
+        so the operator forms of batched runs are not built."""
         lib = _lib.load()
         self._lib = lib
         self.mode = _mode_code(solver_mode)
@@ -91,9 +93,10 @@ class Plan:
         if gl_lookup is not None:
             node, typ = dof_maps_from_lookup(gl_lookup, n)
         handle = ctypes.c_void_p()
-        st = lib.bfe_plan_create(ctypes.byref(Ks), ctypes.byref(Cs), ctypes.byref(Ms), self.dt,
-                                 self.mode, self.precision, ptr(node, ctypes.c_int64),
-                                 ptr(typ, ctypes.c_int32), ctypes.byref(handle))
+        st = lib.bfe_plan_create_ex(ctypes.byref(Ks), ctypes.byref(Cs), ctypes.byref(Ms), self.dt,
+                                    self.mode, self.precision, ptr(node, ctypes.c_int64),
+                                    ptr(typ, ctypes.c_int32),
+                                    _lib.BFE_PLAN_ONE_SOURCE if one_source else 0, ctypes.byref(handle))
         check(st)
         self._h = handle
         nn = ctypes.c_int64()
@@ -405,7 +408,7 @@ def fn_explicit_dynamic_solver_gb300(K, C, M, time, forcing_indices, forcing_fun
     # node information serves the FP32 difference form; an FP64 plan would
     # only use it for many-source kernels, which one load step never runs
     single = _precision_code(solver_precision) == _lib.BFE_PREC_SINGLE
-    with Plan(K, C, M, dt, solver_mode, solver_precision, gl_lookup if single else None) as plan:
+    with Plan(K, C, M, dt, solver_mode, solver_precision, gl_lookup if single else None, one_source=True) as plan:
         hist, fld, fld_t = plan.run(time, forcing_indices, forcing_functions, history_indices,
                                     field_output_every_n_frames, is_vel)
     if history_indices is None or len(np.ravel(history_indices)) == 0:
@@ -433,7 +436,7 @@ def fn_explicit_dynamic_solver_v5_gb300(K, C, M, time, forcing_indices, forcing_
     time = np.asarray(time, float).ravel()
     dt = time[1] - time[0]
     single = _precision_code(solver_precision) == _lib.BFE_PREC_SINGLE
-    with Plan(K, C, M, dt, V5, solver_precision, gl_lookup if single else None) as plan:
+    with Plan(K, C, M, dt, V5, solver_precision, gl_lookup if single else None, one_source=True) as plan:
         hist, fld, frc, fld_t = plan.run_v5(time, forcing_indices, forcing_functions, disp_indices,
                                             disp_functions, history_indices,
                                             field_output_every_n_frames)

@@ -457,9 +457,19 @@ int bfe_plan_destroy(bfe_plan* plan) {
 int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse* Mv,
                     double dt, int32_t solver_mode, int32_t precision,
                     const int64_t* dof_node, const int32_t* dof_type, bfe_plan** out) {
+  return bfe_plan_create_ex(Kv, Cv, Mv, dt, solver_mode, precision, dof_node, dof_type, 0, out);
+}
+
+int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse* Mv,
+                       double dt, int32_t solver_mode, int32_t precision,
+                       const int64_t* dof_node, const int32_t* dof_type, uint32_t flags, bfe_plan** out) {
   g_last_error.clear();
   if (!out) return fail(BFE_ERR_ARG, "out is NULL");
   *out = nullptr;
+  if (flags & ~(uint32_t)BFE_PLAN_ONE_SOURCE) return fail(BFE_ERR_ARG, "unknown plan flags 0x%x", flags);
+  // the node-block and group block-sparse forms serve only runs with many
+  // right-hand sides; a one-source plan skips building them
+  const bool batched_forms = !(flags & BFE_PLAN_ONE_SOURCE);
   if (solver_mode != BFE_MODE_VEL_CURRENT && solver_mode != BFE_MODE_VEL_LAST_HALF &&
       solver_mode != BFE_MODE_V5)
     return fail(BFE_ERR_ARG, "unknown solver_mode %d", solver_mode);
@@ -648,7 +658,7 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   // Node-block form of the FP32 operator: every row must use the difference
   // form, node blocks must hold at most 3 DOFs, and every non-zero coupling
   // to a neighbour DOF type must exist in the own block.
-  if (precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0) {
+  if (batched_forms && precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0) {
     bool ok = true;
     std::vector<uint32_t> hw, hg;
     std::vector<int32_t> hnp(1, 0), hcp(1, 0);
@@ -712,7 +722,7 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   // coefficients Lp. FP64: the direct form, the node's own block included,
   // coefficients of B with its diagonal.
   const bool f64 = precision == BFE_PREC_DOUBLE;
-  if (nodes_ok && (f64 || (have_nodes && direct_rows == 0))) {
+  if (batched_forms && nodes_ok && (f64 || (have_nodes && direct_rows == 0))) {
     // DOF types as dense ids (sorted), the types K couples, their groups
     std::vector<int32_t> type_list(dof_type, dof_type + n);
     std::sort(type_list.begin(), type_list.end());

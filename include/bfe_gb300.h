@@ -91,6 +91,22 @@ int bfe_plan_create(const bfe_sparse* K, const bfe_sparse* C, const bfe_sparse* 
                     const int64_t* dof_node, const int32_t* dof_type,
                     bfe_plan** out);
 
+/* Plan flags of bfe_plan_create_ex. */
+enum {
+  /* The plan serves one source per run (the drop-in call of
+   * fn_explicit_dynamic_solver_v6.m for one load step): the operator forms
+   * used only by runs with many right-hand sides (node blocks, group
+   * block-sparse arrays) are not built, which shortens plan creation.
+   * Batched runs on such a plan still work, through the generic kernel. */
+  BFE_PLAN_ONE_SOURCE = 1
+};
+
+/* bfe_plan_create with flags (0 = bfe_plan_create). */
+int bfe_plan_create_ex(const bfe_sparse* K, const bfe_sparse* C, const bfe_sparse* M,
+                       double dt, int32_t solver_mode, int32_t precision,
+                       const int64_t* dof_node, const int32_t* dof_type, uint32_t flags,
+                       bfe_plan** out);
+
 /*
  * One plan over several independent models (sub-domain and scatterer models,
  * subdoms/fn_run_subdomain_model.m:26-116, which the reference runs one after

@@ -85,6 +85,11 @@ def test_bad_arguments_are_rejected_on_host():
     bad = sp.csr_matrix(np.diag([1.0, np.nan, 1.0, 1.0]))
     st, _ = _create(L, lib, bad, C, M)
     assert st == L.BFE_ERR_NUMERIC
+    ks, k_ = _view(L, K); cs, c_ = _view(L, C); ms, m_ = _view(L, M)
+    h = ctypes.c_void_p()
+    st = lib.bfe_plan_create_ex(ctypes.byref(ks), ctypes.byref(cs), ctypes.byref(ms), 1e-8, 0, 0, None, None,
+                                0x6, ctypes.byref(h))
+    assert st == L.BFE_ERR_ARG and b"flags" in lib.bfe_last_error()
 
 
 def test_null_plan_calls_fail_cleanly():

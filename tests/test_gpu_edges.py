@@ -102,3 +102,27 @@ def test_repeated_monitors_get_the_same_history(bfe, plate):
                                                        "KE", osolver.VEL_CURRENT, "double")
     assert np.array_equal(h1[0], h1[1]) and np.array_equal(h1[1], h1[2])
     assert _err(h1, h0) <= TOL["double"]
+
+
+@pytest.mark.parametrize("prec", ["double", "single"])
+def test_one_source_plan(bfe, plate, prec):
+    """A plan built with BFE_PLAN_ONE_SOURCE (no batched operator forms)
+    gives the one-source results of a full plan bit for bit, and a batched run
+    on it (the generic kernel) matches the oracle."""
+    m = plate
+    t, s = modelgen.pulse(200, m["dt"])
+    nds = m["mon_nds"]
+    fi = modelgen.gi_of(m["gl"], [m["frc_nd"]], 2)
+    hi = modelgen.gi_of(m["gl"], nds, 2)
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, prec, m["gl"]) as full:
+        h_full, f_full, _ = full.run(t, fi, s, hi, 50)
+    srcs = [modelgen.gi_of(m["gl"], [nds[r % nds.size]], 1 + r % 2) for r in range(64)]
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, prec, m["gl"], one_source=True) as one:
+        h_one, f_one, _ = one.run(t, fi, s, hi, 50)
+        hb = one.run_batched(t, srcs, s, hi)
+        st = one.stats()
+    assert np.array_equal(h_one, h_full) and np.array_equal(f_one, f_full)
+    assert st["n_groups"] == 0
+    for r in (0, 63):
+        h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
+        assert _err(hb[:, :, r], h0) <= TOL[prec], r
