@@ -1336,6 +1336,7 @@ bool batched_variant_supported(int precision, int R, int variant, bool have_node
   if (precision == 1 && (R == 16 || R == 32)) return variant == 0 || variant >= 16;
   if (precision == 0) return variant == 0 || (variant == 1 && R % 64 == 0) || (variant == 2 && R % 32 == 0) ||
                              variant == 3;
+  if ((variant == 4 || variant == 5) && !have_nodes) return false;   // node-block form not built
   return true;
 }
 

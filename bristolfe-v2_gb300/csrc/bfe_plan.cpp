@@ -15,6 +15,7 @@
 #include <memory>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda.h>
@@ -35,6 +36,40 @@ int fail(int code, const char* fmt, ...) {
   va_end(ap);
   g_last_error = buf;
   return code;
+}
+
+// Host threads for plan building: the machine's hardware threads (at most
+// 64), and at most one per `grain` work items.
+int plan_threads(int64_t items, int64_t grain) {
+  const unsigned hc = std::thread::hardware_concurrency();
+  int64_t t = std::min<int64_t>(hc ? hc : 1, 64);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(t, items / std::max<int64_t>(grain, 1)));
+}
+
+// Runs f(t, begin, end) for the nt even chunks of [0, items), chunk t on a
+// thread of its own (on the calling thread if a thread cannot be started).
+// No exception leaves a worker: false if any chunk threw (allocation).
+template <typename F>
+bool parallel_chunks(int64_t items, int nt, F&& f) {
+  std::atomic<bool> ok{true};
+  auto run = [&](int t) {
+    try {
+      f(t, items * t / nt, items * (t + 1) / nt);
+    } catch (...) {
+      ok = false;
+    }
+  };
+  std::vector<std::thread> th;
+  int started = 1;
+  try {
+    th.reserve(nt);
+    for (; started < nt; ++started) th.emplace_back(run, started);
+  } catch (...) {
+  }
+  run(0);
+  for (int t = started; t < nt; ++t) run(t);
+  for (auto& x : th) x.join();
+  return ok;
 }
 
 #define CUDA_TRY(expr)                                                                \
@@ -460,27 +495,29 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
   return bfe_plan_create_ex(Kv, Cv, Mv, dt, solver_mode, precision, dof_node, dof_type, 0, out);
 }
 
-int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse* Mv,
-                       double dt, int32_t solver_mode, int32_t precision,
-                       const int64_t* dof_node, const int32_t* dof_type, uint32_t flags, bfe_plan** out) {
-  g_last_error.clear();
-  if (!out) return fail(BFE_ERR_ARG, "out is NULL");
-  *out = nullptr;
+}  // extern "C"
+
+namespace {
+
+// Plan creation from owned CSR matrices (bfe_plan_create_ex converts its
+// views; bfe_plan_create_multi hands over the joined operator).
+int create_plan(Csr K, Csr C, Csr M, double dt, int32_t solver_mode, int32_t precision,
+                const int64_t* dof_node, const int32_t* dof_type, uint32_t flags, bfe_plan** out) {
   if (flags & ~(uint32_t)BFE_PLAN_ONE_SOURCE) return fail(BFE_ERR_ARG, "unknown plan flags 0x%x", flags);
   // the node-block and group block-sparse forms serve only runs with many
   // right-hand sides; a one-source plan skips building them
   const bool batched_forms = !(flags & BFE_PLAN_ONE_SOURCE);
+  // a forced node-block variant (BFE_VARIANT = 4 or 5, the variant sweeps and
+  // tests) needs the node-block form even where the group form exists
+  const char* forced_variant = getenv("BFE_VARIANT");
+  const bool node_form_forced = forced_variant && (atoi(forced_variant) == 4 || atoi(forced_variant) == 5);
   if (solver_mode != BFE_MODE_VEL_CURRENT && solver_mode != BFE_MODE_VEL_LAST_HALF &&
       solver_mode != BFE_MODE_V5)
     return fail(BFE_ERR_ARG, "unknown solver_mode %d", solver_mode);
   if (precision != BFE_PREC_DOUBLE && precision != BFE_PREC_SINGLE)
     return fail(BFE_ERR_ARG, "unknown precision %d", precision);
   if (!(dt > 0) || !std::isfinite(dt)) return fail(BFE_ERR_ARG, "dt must be positive and finite");
-  Csr K, C, M;
   int rc;
-  if ((rc = to_csr(Kv, "K", K))) return rc;
-  if ((rc = to_csr(Cv, "C", C))) return rc;
-  if ((rc = to_csr(Mv, "M", M))) return rc;
   if (K.n != K.m) return fail(BFE_ERR_ARG, "K must be square matrix");
   if (C.n != C.m) return fail(BFE_ERR_ARG, "C must be square matrix");
   if (M.n != M.m) return fail(BFE_ERR_ARG, "M must be square matrix");
@@ -556,6 +593,7 @@ int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_spa
     // every node's rows must be one consecutive block
     std::sort(block_nodes.begin(), block_nodes.end());
     if (std::adjacent_find(block_nodes.begin(), block_nodes.end()) != block_nodes.end()) nodes_ok = false;
+    if (nodes_ok) pl->n_nodes = (int32_t)block_nodes.size();
   }
   const bool have_nodes = precision == BFE_PREC_SINGLE && nodes_ok;
   // diagonal term of B in the FP64 form (v6.m:131-138 with the diagonal of P)
@@ -563,102 +601,354 @@ int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_spa
     return solver_mode == BFE_MODE_VEL_CURRENT ? 2.0 * pdiag[i] : (2.0 - dt * cdiag[i] / m[i]);
   };
 
-  // pack rows into the sliced ELL layout
+  // pack rows into the sliced ELL layout: threads pack contiguous ranges of
+  // slices into pieces of their own, which are then concatenated in order
   const int64_t n_slices = (n + bfe::kSlice - 1) / bfe::kSlice;
   pl->n_slices = (int32_t)n_slices;
-  std::vector<int32_t> sptr(n_slices + 1, 0);
-  std::vector<std::vector<std::pair<uint32_t, double>>> rows(bfe::kSlice);
-  std::vector<uint32_t> hcol;
-  std::vector<unsigned char> hval;
+  const bool f64_ops = precision == BFE_PREC_DOUBLE;
+  struct Piece {
+    std::vector<uint32_t> col;
+    std::vector<double> vd;
+    std::vector<float> vf;
+    std::vector<int64_t> width;
+    int64_t stored = 0, direct = 0;
+  };
   pl->h_base.assign(n, 0);
-  int64_t stored = 0, direct_rows = 0;
-  for (int64_t s = 0; s < n_slices; ++s) {
-    size_t w = 0;
-    for (int r = 0; r < bfe::kSlice; ++r) {
-      rows[r].clear();
-      const int64_t i = s * bfe::kSlice + r;
-      if (i >= n) continue;
-      if (precision == BFE_PREC_DOUBLE) {
-        bool has_diag = false;
-        for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
-          const int64_t j = K.idx[e];
-          double v = -lscale[i] * K.val[e];
-          if (j == i) {
-            v += diag_term(i);
-            has_diag = true;
-          }
-          rows[r].emplace_back((uint32_t)j, v);
-        }
-        if (!has_diag) {
-          const double v = diag_term(i);
-          rows[r].emplace_back((uint32_t)i, v);
-          std::sort(rows[r].begin(), rows[r].end());
-        }
-      } else {
-        // difference form if every column's DOF type exists in the row's
-        // node block and every per-type partial row sum of K vanishes
-        bool diff = have_nodes;
-        if (diff) {
-          // per DOF type of the columns: (type, sum, abs sum); few types per row
-          int32_t ty[16];
-          double sm[16], sa[16];
-          int nty = 0;
-          for (int64_t e = K.ptr[i]; e < K.ptr[i + 1] && diff; ++e) {
-            const int32_t t = dof_type[K.idx[e]];
-            int k = 0;
-            while (k < nty && ty[k] != t) ++k;
-            if (k == nty) {
-              if (nty == 16) { diff = false; break; }
-              ty[nty] = t; sm[nty] = 0.0; sa[nty] = 0.0; ++nty;
-            }
-            sm[k] += K.val[e];
-            sa[k] += std::fabs(K.val[e]);
-          }
-          for (int k = 0; k < nty && diff; ++k) {
-            bool found = false;
-            for (int64_t b = blk_base[i]; b < blk_base[i] + blk_len[i]; ++b)
-              if (dof_type[b] == ty[k]) found = true;
-            if (!found || std::fabs(sm[k]) > 1e-9 * sa[k]) diff = false;
-          }
-        }
-        if (diff) {
-          pl->h_base[i] = (uint32_t)blk_base[i];
+  const int n_pack = plan_threads(n_slices, 1024);
+  std::vector<Piece> pieces(n_pack);
+  const bool packed = parallel_chunks(n_slices, n_pack, [&](int t, int64_t s0, int64_t s1) {
+    Piece& pc = pieces[t];
+    std::vector<std::pair<uint32_t, double>> rows[bfe::kSlice];
+    for (int64_t s = s0; s < s1; ++s) {
+      size_t w = 0;
+      for (int r = 0; r < bfe::kSlice; ++r) {
+        rows[r].clear();
+        const int64_t i = s * bfe::kSlice + r;
+        if (i >= n) continue;
+        if (f64_ops) {
+          bool has_diag = false;
           for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
             const int64_t j = K.idx[e];
-            if (dof_node[j] == dof_node[i]) continue;   // own node block cancels
-            uint32_t slot = 0;
-            for (int64_t k = blk_base[i]; k < blk_base[i] + blk_len[i]; ++k)
-              if (dof_type[k] == dof_type[j]) slot = (uint32_t)(k - blk_base[i]);
-            rows[r].emplace_back((uint32_t)j | (slot << bfe::kSlotShift), lscale[i] * K.val[e]);
+            double v = -lscale[i] * K.val[e];
+            if (j == i) {
+              v += diag_term(i);
+              has_diag = true;
+            }
+            rows[r].emplace_back((uint32_t)j, v);
+          }
+          if (!has_diag) {
+            const double v = diag_term(i);
+            rows[r].emplace_back((uint32_t)i, v);
+            std::sort(rows[r].begin(), rows[r].end());
           }
         } else {
-          ++direct_rows;
-          for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e)
-            rows[r].emplace_back((uint32_t)K.idx[e] | bfe::kDirect, lscale[i] * K.val[e]);
+          // difference form if every column's DOF type exists in the row's
+          // node block and every per-type partial row sum of K vanishes
+          bool diff = have_nodes;
+          if (diff) {
+            // per DOF type of the columns: (type, sum, abs sum); few types per row
+            int32_t ty[16];
+            double sm[16], sa[16];
+            int nty = 0;
+            for (int64_t e = K.ptr[i]; e < K.ptr[i + 1] && diff; ++e) {
+              const int32_t tj = dof_type[K.idx[e]];
+              int k = 0;
+              while (k < nty && ty[k] != tj) ++k;
+              if (k == nty) {
+                if (nty == 16) { diff = false; break; }
+                ty[nty] = tj; sm[nty] = 0.0; sa[nty] = 0.0; ++nty;
+              }
+              sm[k] += K.val[e];
+              sa[k] += std::fabs(K.val[e]);
+            }
+            for (int k = 0; k < nty && diff; ++k) {
+              bool found = false;
+              for (int64_t b = blk_base[i]; b < blk_base[i] + blk_len[i]; ++b)
+                if (dof_type[b] == ty[k]) found = true;
+              if (!found || std::fabs(sm[k]) > 1e-9 * sa[k]) diff = false;
+            }
+          }
+          if (diff) {
+            pl->h_base[i] = (uint32_t)blk_base[i];
+            for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) {
+              const int64_t j = K.idx[e];
+              if (dof_node[j] == dof_node[i]) continue;   // own node block cancels
+              uint32_t slot = 0;
+              for (int64_t k = blk_base[i]; k < blk_base[i] + blk_len[i]; ++k)
+                if (dof_type[k] == dof_type[j]) slot = (uint32_t)(k - blk_base[i]);
+              rows[r].emplace_back((uint32_t)j | (slot << bfe::kSlotShift), lscale[i] * K.val[e]);
+            }
+          } else {
+            ++pc.direct;
+            for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e)
+              rows[r].emplace_back((uint32_t)K.idx[e] | bfe::kDirect, lscale[i] * K.val[e]);
+          }
+        }
+        pc.stored += (int64_t)rows[r].size();
+        w = std::max(w, rows[r].size());
+      }
+      for (size_t k = 0; k < w; ++k) {
+        for (int r = 0; r < bfe::kSlice; ++r) {
+          const int64_t i = s * bfe::kSlice + r;
+          uint32_t c;
+          double v;
+          if (k < rows[r].size()) { c = rows[r][k].first; v = rows[r][k].second; }
+          else { c = (uint32_t)std::min<int64_t>(i, n - 1) | (f64_ops ? 0u : bfe::kDirect); v = 0.0; }
+          pc.col.push_back(c);
+          if (f64_ops) pc.vd.push_back(v); else pc.vf.push_back((float)v);
         }
       }
-      stored += (int64_t)rows[r].size();
-      w = std::max(w, rows[r].size());
+      pc.width.push_back((int64_t)w);
     }
-    for (size_t k = 0; k < w; ++k) {
-      for (int r = 0; r < bfe::kSlice; ++r) {
-        const int64_t i = s * bfe::kSlice + r;
-        uint32_t c;
-        double v;
-        if (k < rows[r].size()) { c = rows[r][k].first; v = rows[r][k].second; }
-        else { c = (uint32_t)std::min<int64_t>(i, n - 1) | (precision == BFE_PREC_SINGLE ? bfe::kDirect : 0u); v = 0.0; }
-        hcol.push_back(c);
-        if (precision == BFE_PREC_DOUBLE) push_val<double>(hval, v); else push_val<float>(hval, v);
+  });
+  if (!packed) return fail(BFE_ERR_OOM, "host allocation failed while packing the operator");
+  std::vector<int32_t> sptr(n_slices + 1, 0);
+  int64_t stored = 0, direct_rows = 0, total = 0;
+  {
+    int64_t s = 0;
+    for (const Piece& pc : pieces) {
+      for (int64_t w : pc.width) {
+        total += w * bfe::kSlice;
+        if (total > (int64_t)INT32_MAX) return fail(BFE_ERR_UNSUPPORTED, "operator too large for 32-bit offsets");
+        sptr[++s] = (int32_t)total;
+        pl->max_slice_entries = std::max<int32_t>(pl->max_slice_entries, (int32_t)(w * bfe::kSlice));
+      }
+      stored += pc.stored;
+      direct_rows += pc.direct;
+    }
+  }
+  const size_t es_ops = f64_ops ? sizeof(double) : sizeof(float);
+  std::vector<uint32_t> hcol((size_t)total);
+  std::vector<unsigned char> hval((size_t)total * es_ops);
+  {
+    size_t o = 0;
+    for (Piece& pc : pieces) {
+      const size_t k = pc.col.size();
+      if (k) {
+        std::memcpy(hcol.data() + o, pc.col.data(), k * sizeof(uint32_t));
+        std::memcpy(hval.data() + o * es_ops, f64_ops ? (const void*)pc.vd.data() : (const void*)pc.vf.data(),
+                    k * es_ops);
+      }
+      o += k;
+      pc = Piece();
+    }
+  }
+  // Group block-sparse form: DOF types coupled by K form groups; each group
+  // becomes a block-sparse matrix with BS x BS blocks over the nodes that
+  // carry it (requires consecutive group rows inside each node block). FP32:
+  // the difference form on every row, blocks of the neighbour nodes only,
+  // coefficients Lp. FP64: the direct form, the node's own block included,
+  // coefficients of B with its diagonal.
+  const bool f64 = precision == BFE_PREC_DOUBLE;
+  if (batched_forms && nodes_ok && (f64 || (have_nodes && direct_rows == 0))) {
+    // DOF types as dense ids (sorted), the types K couples, their groups
+    std::vector<int32_t> type_list(dof_type, dof_type + n);
+    std::sort(type_list.begin(), type_list.end());
+    type_list.erase(std::unique(type_list.begin(), type_list.end()), type_list.end());
+    const int nt_ = (int)type_list.size();
+    bool ok = nt_ <= 3 * bfe::kMaxGroups;
+    std::vector<uint8_t> tid(n, 0);
+    if (ok)
+      for (int64_t i = 0; i < n; ++i)
+        tid[i] = (uint8_t)(std::lower_bound(type_list.begin(), type_list.end(), dof_type[i]) - type_list.begin());
+    std::vector<int> parent(std::max(nt_, 1));
+    for (int t = 0; t < nt_; ++t) parent[t] = t;
+    auto find = [&](int x) {
+      while (parent[x] != x) x = parent[x] = parent[parent[x]];
+      return x;
+    };
+    if (ok) {
+      // type pairs K couples (row chunks on threads, tables OR-ed)
+      const int n_cpl = plan_threads(n, 1 << 16);
+      std::vector<std::vector<char>> cpl(n_cpl, std::vector<char>((size_t)nt_ * nt_, 0));
+      if (!parallel_chunks(n, n_cpl, [&](int t, int64_t i0, int64_t i1) {
+            char* c = cpl[t].data();
+            for (int64_t i = i0; i < i1; ++i)
+              for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) c[(size_t)tid[i] * nt_ + tid[K.idx[e]]] = 1;
+          }))
+        return fail(BFE_ERR_OOM, "host allocation failed while building the group operator");
+      std::vector<char> coupled((size_t)nt_ * nt_, 0);
+      for (const auto& c : cpl)
+        for (size_t k = 0; k < c.size(); ++k) coupled[k] |= c[k];
+      for (int a1 = 0; a1 < nt_; ++a1)
+        for (int b1 = 0; b1 < nt_; ++b1)
+          if (coupled[(size_t)a1 * nt_ + b1]) {
+            const int ra = find(a1), rb = find(b1);
+            if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
+          }
+    }
+    std::map<int, std::vector<int32_t>> gtypes;         // root -> sorted types
+    for (int t = 0; t < nt_ && ok; ++t) gtypes[find(t)].push_back(type_list[t]);
+    ok = ok && gtypes.size() <= (size_t)bfe::kMaxGroups;
+    std::vector<std::vector<int32_t>> types;
+    for (auto& kv : gtypes) { types.push_back(kv.second); if (kv.second.size() > 3) ok = false; }
+    std::vector<std::pair<int, int>> tpos(std::max(nt_, 1));   // dense type -> (group, position)
+    for (size_t gi = 0; gi < types.size(); ++gi)
+      for (size_t k = 0; k < types[gi].size(); ++k) {
+        const int t = (int)(std::lower_bound(type_list.begin(), type_list.end(), types[gi][k]) - type_list.begin());
+        tpos[t] = {(int)gi, (int)k};
+      }
+    auto type_pos_of = [&](int64_t dof) { return tpos[tid[dof]]; };
+    std::vector<std::vector<int32_t>> row0s(types.size());
+    // every node block: each group it touches must be complete and consecutive
+    for (int64_t b = 0; b < n && ok; b += blk_len[b]) {
+      for (int64_t k = b; k < b + blk_len[b]; ++k) {
+        const auto tp = type_pos_of(k);
+        if (tp.second != 0) continue;
+        const auto& ty = types[tp.first];
+        if (k + (int64_t)ty.size() > b + blk_len[b]) { ok = false; break; }
+        for (size_t l = 0; l < ty.size(); ++l)
+          if (dof_type[k + l] != ty[l]) ok = false;
+        row0s[tp.first].push_back((int32_t)k);
+      }
+      for (int64_t k = b; k < b + blk_len[b]; ++k) {
+        const auto tp = type_pos_of(k);
+        if (tp.second != 0 && (k - tp.second < b || dof_type[k - tp.second] != types[tp.first][0])) ok = false;
       }
     }
-    sptr[s + 1] = (int32_t)hcol.size();
-    if (hcol.size() > (size_t)INT32_MAX) return fail(BFE_ERR_UNSUPPORTED, "operator too large for 32-bit offsets");
-    pl->max_slice_entries = std::max<int32_t>(pl->max_slice_entries, (int32_t)(w * bfe::kSlice));
+    if (ok) {
+      int32_t blocks = 0;
+      pl->groups.n_groups = (int32_t)types.size();
+      for (size_t gi = 0; gi < types.size() && ok; ++gi) {
+        const int bs = (int)types[gi].size();
+        const std::vector<int32_t>& nodes = row0s[gi];
+        // threads build contiguous ranges of the group's nodes: per node its
+        // neighbour blocks (sorted) and their BS x BS coefficients; each row's
+        // sorted columns are merged with the sorted block columns
+        struct GPiece {
+          std::vector<int32_t> cnt, nrow;
+          std::vector<float> coef;
+          std::vector<double> coef64;
+        };
+        const int n_grp = plan_threads((int64_t)nodes.size(), 2048);
+        std::vector<GPiece> gp(n_grp);
+        const bool built = parallel_chunks((int64_t)nodes.size(), n_grp, [&](int t, int64_t q0, int64_t q1) {
+          GPiece& pc = gp[t];
+          std::vector<int64_t> nb_rows;
+          for (int64_t q = q0; q < q1; ++q) {
+            const int32_t a0 = nodes[q];
+            nb_rows.clear();
+            if (f64) nb_rows.push_back(a0);
+            for (int k = 0; k < bs; ++k)
+              for (int64_t e = K.ptr[a0 + k]; e < K.ptr[a0 + k + 1]; ++e) {
+                const int64_t j = K.idx[e];
+                if (!f64 && dof_node[j] == dof_node[a0]) continue;
+                nb_rows.push_back(j - type_pos_of(j).second);
+              }
+            std::sort(nb_rows.begin(), nb_rows.end());
+            nb_rows.erase(std::unique(nb_rows.begin(), nb_rows.end()), nb_rows.end());
+            int64_t ek[3];
+            for (int k = 0; k < bs; ++k) ek[k] = K.ptr[a0 + k];
+            for (int64_t b0 : nb_rows) {
+              pc.nrow.push_back((int32_t)b0);
+              for (int k = 0; k < bs; ++k) {
+                const int64_t row = a0 + k, end = K.ptr[row + 1];
+                for (int l = 0; l < bs; ++l) {
+                  const int64_t col = b0 + l;
+                  while (ek[k] < end && K.idx[ek[k]] < col) ++ek[k];
+                  const double kv = ek[k] < end && K.idx[ek[k]] == col ? K.val[ek[k]] : 0.0;
+                  if (f64) pc.coef64.push_back(-lscale[row] * kv + (row == col ? diag_term(row) : 0.0));
+                  else pc.coef.push_back(kv != 0.0 ? (float)(lscale[row] * kv) : 0.0f);
+                }
+              }
+            }
+            pc.cnt.push_back((int32_t)nb_rows.size());
+          }
+        });
+        if (!built) return fail(BFE_ERR_OOM, "host allocation failed while building the group operator");
+        std::vector<int32_t> nptr(1, 0), nrow;
+        std::vector<float> coef;
+        std::vector<double> coef64;
+        {
+          size_t n_blk = 0;
+          for (const GPiece& pc : gp) n_blk += pc.nrow.size();
+          if (n_blk * bs * bs >= (size_t)INT32_MAX) { ok = false; break; }
+          nptr.reserve(nodes.size() + 1);
+          nrow.reserve(n_blk);
+          if (f64) coef64.reserve(n_blk * bs * bs);
+          else coef.reserve(n_blk * bs * bs);
+          for (GPiece& pc : gp) {
+            for (int32_t c : pc.cnt) nptr.push_back(nptr.back() + c);
+            nrow.insert(nrow.end(), pc.nrow.begin(), pc.nrow.end());
+            coef.insert(coef.end(), pc.coef.begin(), pc.coef.end());
+            coef64.insert(coef64.end(), pc.coef64.begin(), pc.coef64.end());
+            pc = GPiece();
+          }
+        }
+        pl->groups.bs[gi] = bs;
+        pl->groups.n_nodes[gi] = (int32_t)row0s[gi].size();
+        pl->groups.blk_begin[gi] = blocks;
+        blocks += (int32_t)((row0s[gi].size() + 7) / 8);
+        CUDA_TRY(pl->g_row0[gi].upload(row0s[gi]));
+        CUDA_TRY(pl->g_nptr[gi].upload(nptr));
+        CUDA_TRY(pl->g_nrow[gi].upload(nrow));
+        std::vector<int4> rec(row0s[gi].size());
+        for (size_t a0 = 0; a0 < rec.size(); ++a0)
+          rec[a0] = make_int4(row0s[gi][a0], nptr[a0], nptr[a0 + 1] - nptr[a0], 0);
+        CUDA_TRY(pl->g_rec[gi].upload(rec));
+        pl->groups.rec[gi] = pl->g_rec[gi].p;
+        pl->groups.row0[gi] = pl->g_row0[gi].p;
+        pl->groups.nptr[gi] = pl->g_nptr[gi].p;
+        pl->groups.nrow[gi] = pl->g_nrow[gi].p;
+        if (f64) {
+          CUDA_TRY(pl->g_coef64[gi].upload(coef64));
+          pl->groups.coef64[gi] = pl->g_coef64[gi].p;
+          continue;
+        }
+        CUDA_TRY(pl->g_coef[gi].upload(coef));
+        // flat neighbour rows, broadcast pairs and the padded pair copy (each
+        // node's pairs start on a 16-byte boundary), filled on threads
+        const int64_t n_nodes_g = (int64_t)nodes.size();
+        std::vector<int32_t> frow(nrow.size() * bs);
+        std::vector<float2> coef2(coef.size());
+        std::vector<int32_t> cofs(n_nodes_g);
+        size_t n_pairs = 0;
+        for (int64_t a0 = 0; a0 < n_nodes_g; ++a0) {
+          n_pairs += n_pairs & 1;
+          cofs[a0] = (int32_t)n_pairs;
+          n_pairs += (size_t)(nptr[a0 + 1] - nptr[a0]) * bs * bs;
+        }
+        n_pairs += n_pairs & 1;
+        if (n_pairs >= (size_t)INT32_MAX) return fail(BFE_ERR_UNSUPPORTED, "group operator too large");
+        std::vector<float2> coefp(std::max<size_t>(n_pairs, 1), make_float2(0.f, 0.f));
+        const int n_fill = plan_threads(n_nodes_g, 4096);
+        if (!parallel_chunks(n_nodes_g, n_fill, [&](int, int64_t q0, int64_t q1) {
+              for (int64_t a0 = q0; a0 < q1; ++a0) {
+                for (int32_t b = nptr[a0]; b < nptr[a0 + 1]; ++b)
+                  for (int l = 0; l < bs; ++l) frow[(size_t)b * bs + l] = nrow[b] + l;
+                const size_t c0 = (size_t)nptr[a0] * bs * bs, c1 = (size_t)nptr[a0 + 1] * bs * bs;
+                for (size_t k = c0; k < c1; ++k) {
+                  coef2[k] = make_float2(coef[k], coef[k]);
+                  coefp[cofs[a0] + (k - c0)] = coef2[k];
+                }
+              }
+            }))
+          return fail(BFE_ERR_OOM, "host allocation failed while building the group operator");
+        CUDA_TRY(pl->g_frow[gi].upload(frow));
+        pl->groups.frow[gi] = pl->g_frow[gi].p;
+        CUDA_TRY(pl->g_coef2[gi].upload(coef2));
+        pl->groups.coef2[gi] = pl->g_coef2[gi].p;
+        CUDA_TRY(pl->g_cofs[gi].upload(cofs));
+        CUDA_TRY(pl->g_coefp[gi].upload(coefp));
+        pl->tma.cofs[gi] = pl->g_cofs[gi].p;
+        pl->tma.coefp[gi] = pl->g_coefp[gi].p;
+        pl->groups.coef[gi] = pl->g_coef[gi].p;
+      }
+      pl->groups.blk_begin[pl->groups.n_groups] = blocks;
+      pl->have_groups = ok && blocks > 0;
+      if (pl->have_groups && !f64) {
+        CUDA_TRY(pl->d_err.alloc(1));
+        pl->tma.err = pl->d_err.p;
+      }
+    }
   }
-  // Node-block form of the FP32 operator: every row must use the difference
+  // Node-block form of the FP32 operator (kernels step_f32_node, batched
+  // variants 4 and 5), the fallback when the group form cannot be built or
+  // when one of its variants is forced: every row must use the difference
   // form, node blocks must hold at most 3 DOFs, and every non-zero coupling
   // to a neighbour DOF type must exist in the own block.
-  if (batched_forms && precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0) {
+  if (batched_forms && precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0 &&
+      (!pl->have_groups || node_form_forced)) {
     bool ok = true;
     std::vector<uint32_t> hw, hg;
     std::vector<int32_t> hnp(1, 0), hcp(1, 0);
@@ -715,163 +1005,6 @@ int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_spa
       CUDA_TRY(pl->coef.upload(hc));
     }
   }
-  // Group block-sparse form: DOF types coupled by K form groups; each group
-  // becomes a block-sparse matrix with BS x BS blocks over the nodes that
-  // carry it (requires consecutive group rows inside each node block). FP32:
-  // the difference form on every row, blocks of the neighbour nodes only,
-  // coefficients Lp. FP64: the direct form, the node's own block included,
-  // coefficients of B with its diagonal.
-  const bool f64 = precision == BFE_PREC_DOUBLE;
-  if (batched_forms && nodes_ok && (f64 || (have_nodes && direct_rows == 0))) {
-    // DOF types as dense ids (sorted), the types K couples, their groups
-    std::vector<int32_t> type_list(dof_type, dof_type + n);
-    std::sort(type_list.begin(), type_list.end());
-    type_list.erase(std::unique(type_list.begin(), type_list.end()), type_list.end());
-    const int nt_ = (int)type_list.size();
-    bool ok = nt_ <= 3 * bfe::kMaxGroups;
-    std::vector<uint8_t> tid(n, 0);
-    if (ok)
-      for (int64_t i = 0; i < n; ++i)
-        tid[i] = (uint8_t)(std::lower_bound(type_list.begin(), type_list.end(), dof_type[i]) - type_list.begin());
-    std::vector<int> parent(std::max(nt_, 1));
-    for (int t = 0; t < nt_; ++t) parent[t] = t;
-    auto find = [&](int x) {
-      while (parent[x] != x) x = parent[x] = parent[parent[x]];
-      return x;
-    };
-    if (ok) {
-      std::vector<char> coupled((size_t)nt_ * nt_, 0);
-      for (int64_t i = 0; i < n; ++i)
-        for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e) coupled[(size_t)tid[i] * nt_ + tid[K.idx[e]]] = 1;
-      for (int a1 = 0; a1 < nt_; ++a1)
-        for (int b1 = 0; b1 < nt_; ++b1)
-          if (coupled[(size_t)a1 * nt_ + b1]) {
-            const int ra = find(a1), rb = find(b1);
-            if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
-          }
-    }
-    std::map<int, std::vector<int32_t>> gtypes;         // root -> sorted types
-    for (int t = 0; t < nt_ && ok; ++t) gtypes[find(t)].push_back(type_list[t]);
-    ok = ok && gtypes.size() <= (size_t)bfe::kMaxGroups;
-    std::vector<std::vector<int32_t>> types;
-    for (auto& kv : gtypes) { types.push_back(kv.second); if (kv.second.size() > 3) ok = false; }
-    std::vector<std::pair<int, int>> tpos(std::max(nt_, 1));   // dense type -> (group, position)
-    for (size_t gi = 0; gi < types.size(); ++gi)
-      for (size_t k = 0; k < types[gi].size(); ++k) {
-        const int t = (int)(std::lower_bound(type_list.begin(), type_list.end(), types[gi][k]) - type_list.begin());
-        tpos[t] = {(int)gi, (int)k};
-      }
-    auto type_pos_of = [&](int64_t dof) { return tpos[tid[dof]]; };
-    std::vector<std::vector<int32_t>> row0s(types.size());
-    // every node block: each group it touches must be complete and consecutive
-    for (int64_t b = 0; b < n && ok; b += blk_len[b]) {
-      for (int64_t k = b; k < b + blk_len[b]; ++k) {
-        const auto tp = type_pos_of(k);
-        if (tp.second != 0) continue;
-        const auto& ty = types[tp.first];
-        if (k + (int64_t)ty.size() > b + blk_len[b]) { ok = false; break; }
-        for (size_t l = 0; l < ty.size(); ++l)
-          if (dof_type[k + l] != ty[l]) ok = false;
-        row0s[tp.first].push_back((int32_t)k);
-      }
-      for (int64_t k = b; k < b + blk_len[b]; ++k) {
-        const auto tp = type_pos_of(k);
-        if (tp.second != 0 && (k - tp.second < b || dof_type[k - tp.second] != types[tp.first][0])) ok = false;
-      }
-    }
-    if (ok) {
-      int32_t blocks = 0;
-      pl->groups.n_groups = (int32_t)types.size();
-      for (size_t gi = 0; gi < types.size() && ok; ++gi) {
-        const int bs = (int)types[gi].size();
-        std::vector<int32_t> nptr(1, 0), nrow;
-        std::vector<float> coef;
-        std::vector<double> coef64;
-        std::vector<int64_t> nb_rows;
-        for (int32_t a0 : row0s[gi]) {
-          nb_rows.clear();
-          if (f64) nb_rows.push_back(a0);
-          for (int k = 0; k < bs; ++k)
-            for (int64_t e = K.ptr[a0 + k]; e < K.ptr[a0 + k + 1]; ++e) {
-              const int64_t j = K.idx[e];
-              if (!f64 && dof_node[j] == dof_node[a0]) continue;
-              nb_rows.push_back(j - type_pos_of(j).second);
-            }
-          std::sort(nb_rows.begin(), nb_rows.end());
-          nb_rows.erase(std::unique(nb_rows.begin(), nb_rows.end()), nb_rows.end());
-          for (int64_t b0 : nb_rows) {
-            nrow.push_back((int32_t)b0);
-            for (int k = 0; k < bs; ++k) {
-              const int64_t row = a0 + k;
-              const int64_t* beg = K.idx.data() + K.ptr[row];
-              const int64_t* end = K.idx.data() + K.ptr[row + 1];
-              for (int l = 0; l < bs; ++l) {
-                const int64_t* hit = std::lower_bound(beg, end, b0 + l);
-                const double kv = hit != end && *hit == b0 + l ? K.val[hit - K.idx.data()] : 0.0;
-                if (f64) coef64.push_back(-lscale[row] * kv + (row == b0 + l ? diag_term(row) : 0.0));
-                else coef.push_back(kv != 0.0 ? (float)(lscale[row] * kv) : 0.0f);
-              }
-            }
-          }
-          nptr.push_back((int32_t)nrow.size());
-        }
-        if (std::max(coef.size(), coef64.size()) >= (size_t)INT32_MAX) { ok = false; break; }
-        pl->groups.bs[gi] = bs;
-        pl->groups.n_nodes[gi] = (int32_t)row0s[gi].size();
-        pl->groups.blk_begin[gi] = blocks;
-        blocks += (int32_t)((row0s[gi].size() + 7) / 8);
-        CUDA_TRY(pl->g_row0[gi].upload(row0s[gi]));
-        CUDA_TRY(pl->g_nptr[gi].upload(nptr));
-        CUDA_TRY(pl->g_nrow[gi].upload(nrow));
-        std::vector<int4> rec(row0s[gi].size());
-        for (size_t a0 = 0; a0 < rec.size(); ++a0)
-          rec[a0] = make_int4(row0s[gi][a0], nptr[a0], nptr[a0 + 1] - nptr[a0], 0);
-        CUDA_TRY(pl->g_rec[gi].upload(rec));
-        pl->groups.rec[gi] = pl->g_rec[gi].p;
-        pl->groups.row0[gi] = pl->g_row0[gi].p;
-        pl->groups.nptr[gi] = pl->g_nptr[gi].p;
-        pl->groups.nrow[gi] = pl->g_nrow[gi].p;
-        if (f64) {
-          CUDA_TRY(pl->g_coef64[gi].upload(coef64));
-          pl->groups.coef64[gi] = pl->g_coef64[gi].p;
-          continue;
-        }
-        CUDA_TRY(pl->g_coef[gi].upload(coef));
-        std::vector<int32_t> frow;
-        frow.reserve(nrow.size() * bs);
-        for (int32_t r0 : nrow)
-          for (int l = 0; l < bs; ++l) frow.push_back(r0 + l);
-        CUDA_TRY(pl->g_frow[gi].upload(frow));
-        pl->groups.frow[gi] = pl->g_frow[gi].p;
-        std::vector<float2> coef2(coef.size());
-        for (size_t k = 0; k < coef.size(); ++k) coef2[k] = make_float2(coef[k], coef[k]);
-        CUDA_TRY(pl->g_coef2[gi].upload(coef2));
-        pl->groups.coef2[gi] = pl->g_coef2[gi].p;
-        // padded copy: each node's pairs start on a 16-byte boundary
-        std::vector<int32_t> cofs;
-        std::vector<float2> coefp;
-        for (size_t a0 = 0; a0 + 1 < nptr.size(); ++a0) {
-          if (coefp.size() & 1) coefp.push_back(make_float2(0.f, 0.f));
-          cofs.push_back((int32_t)coefp.size());
-          const size_t b0 = (size_t)nptr[a0] * bs * bs, b1 = (size_t)nptr[a0 + 1] * bs * bs;
-          for (size_t k = b0; k < b1; ++k) coefp.push_back(coef2[k]);
-        }
-        if (coefp.size() & 1) coefp.push_back(make_float2(0.f, 0.f));
-        if (coefp.empty()) coefp.push_back(make_float2(0.f, 0.f));
-        CUDA_TRY(pl->g_cofs[gi].upload(cofs));
-        CUDA_TRY(pl->g_coefp[gi].upload(coefp));
-        pl->tma.cofs[gi] = pl->g_cofs[gi].p;
-        pl->tma.coefp[gi] = pl->g_coefp[gi].p;
-        pl->groups.coef[gi] = pl->g_coef[gi].p;
-      }
-      pl->groups.blk_begin[pl->groups.n_groups] = blocks;
-      pl->have_groups = ok && blocks > 0;
-      if (pl->have_groups && !f64) {
-        CUDA_TRY(pl->d_err.alloc(1));
-        pl->tma.err = pl->d_err.p;
-      }
-    }
-  }
   pl->nnz_operator = stored;
   pl->nnz_padded = (int64_t)hcol.size();
   pl->n_direct_rows = direct_rows;
@@ -913,6 +1046,25 @@ int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_spa
   }
   *out = pl.release();
   return BFE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse* Mv,
+                       double dt, int32_t solver_mode, int32_t precision,
+                       const int64_t* dof_node, const int32_t* dof_type, uint32_t flags, bfe_plan** out) {
+  g_last_error.clear();
+  if (!out) return fail(BFE_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  Csr K, C, M;
+  int rc;
+  if ((rc = to_csr(Kv, "K", K))) return rc;
+  if ((rc = to_csr(Cv, "C", C))) return rc;
+  if ((rc = to_csr(Mv, "M", M))) return rc;
+  return create_plan(std::move(K), std::move(C), std::move(M), dt, solver_mode, precision, dof_node, dof_type,
+                     flags, out);
 }
 
 int bfe_plan_create_assembled(const bfe_matrices* mats, double dt, int32_t solver_mode, int32_t precision,
@@ -965,28 +1117,29 @@ int bfe_plan_create_multi(int32_t n_models, const bfe_sparse* K, const bfe_spars
     n += ks[k].n;
     row_offsets[k + 1] = n;
   }
-  auto join = [&](std::vector<Csr>& parts, std::vector<int64_t>& p, std::vector<int64_t>& ix, std::vector<double>& v) {
-    p.assign(1, 0);
+  // join block-diagonally: model k's rows and columns shift by row_offsets[k]
+  auto join = [&](std::vector<Csr>& parts, Csr& J) {
+    size_t nnz = 0;
+    for (const Csr& c : parts) nnz += c.idx.size();
+    J.n = J.m = n;
+    J.ptr.assign(n + 1, 0);
+    J.idx.resize(nnz);
+    J.val.resize(nnz);
+    size_t o = 0;
     for (int32_t k = 0; k < n_models; ++k) {
       const int64_t off = row_offsets[k];
-      for (int64_t i = 0; i < parts[k].n; ++i) {
-        for (int64_t e = parts[k].ptr[i]; e < parts[k].ptr[i + 1]; ++e) {
-          ix.push_back(parts[k].idx[e] + off);
-          v.push_back(parts[k].val[e]);
-        }
-        p.push_back((int64_t)ix.size());
-      }
+      const Csr& c = parts[k];
+      for (int64_t i = 0; i < c.n; ++i) J.ptr[off + i + 1] = (int64_t)o + c.ptr[i + 1];
+      for (size_t e = 0; e < c.idx.size(); ++e) J.idx[o + e] = c.idx[e] + off;
+      if (!c.val.empty()) std::memcpy(J.val.data() + o, c.val.data(), c.val.size() * sizeof(double));
+      o += c.idx.size();
       parts[k] = Csr();
     }
   };
-  std::vector<int64_t> kp, ki, cp, ci, mp, mi;
-  std::vector<double> kv, cv, mv;
-  join(ks, kp, ki, kv);
-  join(cs, cp, ci, cv);
-  join(ms, mp, mi, mv);
-  const bfe_sparse Kj{n, n, (int64_t)kv.size(), BFE_CSR, kp.data(), ki.data(), kv.data()};
-  const bfe_sparse Cj{n, n, (int64_t)cv.size(), BFE_CSR, cp.data(), ci.data(), cv.data()};
-  const bfe_sparse Mj{n, n, (int64_t)mv.size(), BFE_CSR, mp.data(), mi.data(), mv.data()};
+  Csr Kj, Cj, Mj;
+  join(ks, Kj);
+  join(cs, Cj);
+  join(ms, Mj);
   std::vector<int64_t> node;
   std::vector<int32_t> type;
   bool have = dof_node && dof_type;
@@ -1005,8 +1158,9 @@ int bfe_plan_create_multi(int32_t n_models, const bfe_sparse* K, const bfe_spars
       node_base += mx + 1;
     }
   }
-  return bfe_plan_create(&Kj, &Cj, &Mj, dt, solver_mode, precision, have ? node.data() : nullptr,
-                         have ? type.data() : nullptr, out);
+  *out = nullptr;
+  return create_plan(std::move(Kj), std::move(Cj), std::move(Mj), dt, solver_mode, precision,
+                     have ? node.data() : nullptr, have ? type.data() : nullptr, 0, out);
 }
 
 }  // extern "C"
@@ -1188,7 +1342,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   stt.nnz_padded = pl->nnz_padded;
   stt.n_interface = pl->n_int;
   stt.n_direct_rows = pl->n_direct_rows;
-  stt.n_nodes = pl->have_node_blocks ? pl->n_nodes : 0;
+  stt.n_nodes = pl->n_nodes;
   stt.n_groups = pl->have_groups ? pl->groups.n_groups : 0;
   if (prec == BFE_PREC_SINGLE && rs.n_sig > 0) stt.aux_launches += 1;
   // optional per-launch CUDA-event timing: events are recorded around every

@@ -398,8 +398,8 @@ typedef struct bfe_stats {
   int64_t n_interface;       /* rows with fluid-solid coupling */
   int64_t n_direct_rows;     /* FP32 rows evaluated in direct form */
   int64_t variant;           /* batched kernel variant chosen by the autotuner */
-  int64_t n_nodes;           /* node blocks of the FP32 node-block operator (0 = none) */
-  int64_t n_groups;          /* DOF-type groups of the FP32 block-sparse operator (0 = none) */
+  int64_t n_nodes;           /* nodes given by dof_node / dof_type (0 = no node information) */
+  int64_t n_groups;          /* DOF-type groups of the group block-sparse operator (0 = none) */
 } bfe_stats;
 
 /* Enable (1) or disable (0) CUDA-event timing of every launch in later runs. */
