@@ -280,7 +280,7 @@ struct bfe_matrices {
 extern "C" {
 
 int bfe_assemble_2d(const bfe_mesh2d* mesh, int32_t n_mat, const bfe_material* matls,
-                    const bfe_assembly_options* opt, bfe_matrices** out) {
+                    const bfe_assembly_options* opt, bfe_matrices** out) try {
   bfe::set_last_error("");
   if (!out || !mesh || !matls) return afail(BFE_ERR_ARG, "NULL argument");
   *out = nullptr;
@@ -481,6 +481,8 @@ int bfe_assemble_2d(const bfe_mesh2d* mesh, int32_t n_mat, const bfe_material* m
   if (herr) return afail(BFE_ERR_NUMERIC, "a matrix row has non-zeros in a DOF whose column is empty");
   *out = M.release();
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_matrices_info(const bfe_matrices* m, int64_t* n_dof, int64_t* nnz_k, int64_t* nnz_c,
@@ -495,7 +497,7 @@ int bfe_matrices_info(const bfe_matrices* m, int64_t* n_dof, int64_t* nnz_k, int
   return BFE_OK;
 }
 
-int bfe_matrices_copy(const bfe_matrices* m, int32_t which, int64_t* ptr, int64_t* idx, double* val) {
+int bfe_matrices_copy(const bfe_matrices* m, int32_t which, int64_t* ptr, int64_t* idx, double* val) try {
   bfe::set_last_error("");
   if (!m) return afail(BFE_ERR_ARG, "matrices is NULL");
   if (which < 0 || which > 2) return afail(BFE_ERR_ARG, "which must be 0 (K), 1 (C) or 2 (M)");
@@ -513,9 +515,11 @@ int bfe_matrices_copy(const bfe_matrices* m, int32_t which, int64_t* ptr, int64_
   for (int64_t i = 0; i <= nd; ++i) ptr[i] = hp[i];
   for (int64_t k = 0; k < nz; ++k) idx[k] = hc[k];
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
-int bfe_matrices_gl_lookup(const bfe_matrices* m, int64_t* gl_lookup) {
+int bfe_matrices_gl_lookup(const bfe_matrices* m, int64_t* gl_lookup) try {
   bfe::set_last_error("");
   if (!m || !gl_lookup) return afail(BFE_ERR_ARG, "NULL argument");
   int dev = 0;
@@ -528,6 +532,8 @@ int bfe_matrices_gl_lookup(const bfe_matrices* m, int64_t* gl_lookup) {
   for (int64_t a = 0; a < m->n_nodes; ++a)           // [node][dof] -> column-major n_nodes x max_df
     for (int32_t d = 0; d < m->max_df; ++d) gl_lookup[a + m->n_nodes * d] = h[(size_t)a * m->max_df + d];
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_matrices_destroy(bfe_matrices* m) {

@@ -150,7 +150,7 @@ extern "C" {
 
 int bfe_field_create(int32_t type, int32_t component, int64_t n, int64_t n_nodes, int32_t n_dims,
                      const double* nds, int32_t max_df, const int64_t* gl_lookup, int64_t n_el,
-                     int32_t el_cols, const int64_t* els, const double* m_diag, bfe_field** out) {
+                     int32_t el_cols, const int64_t* els, const double* m_diag, bfe_field** out) try {
   bfe::set_last_error("");
   if (!out) return ffail(BFE_ERR_ARG, "out is NULL");
   *out = nullptr;
@@ -244,6 +244,8 @@ int bfe_field_create(int32_t type, int32_t component, int64_t n, int64_t n_nodes
     return ffail(BFE_ERR_CUDA, cudaGetErrorString(ce));
   *out = guard.release();
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_field_destroy(bfe_field* field) {
@@ -251,7 +253,7 @@ int bfe_field_destroy(bfe_field* field) {
   return BFE_OK;
 }
 
-int bfe_field_apply(bfe_field* f, int64_t n_frames, const double* fld, double* out) {
+int bfe_field_apply(bfe_field* f, int64_t n_frames, const double* fld, double* out) try {
   bfe::set_last_error("");
   if (!f) return ffail(BFE_ERR_ARG, "field is NULL");
   if (n_frames < 0) return ffail(BFE_ERR_ARG, "invalid sizes");
@@ -276,6 +278,8 @@ int bfe_field_apply(bfe_field* f, int64_t n_frames, const double* fld, double* o
   if (dev != f->device) cudaSetDevice(dev);
   if (ce != cudaSuccess) return ffail(BFE_ERR_CUDA, cudaGetErrorString(ce));
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 }  // extern "C"

@@ -131,7 +131,7 @@ int launch_convolve(int64_t n_t, int64_t n_sig, const double* d_f, const double*
 
 extern "C" {
 
-int bfe_convolve(int64_t n_t, int64_t n_sig, const double* f, int64_t n_g, const double* g, double* h) {
+int bfe_convolve(int64_t n_t, int64_t n_sig, const double* f, int64_t n_g, const double* g, double* h) try {
   bfe::set_last_error("");
   if (n_t <= 0 || n_sig < 0 || n_g < 0) return ffail(BFE_ERR_ARG, "invalid sizes");
   if (n_sig == 0) return BFE_OK;
@@ -150,12 +150,14 @@ int bfe_convolve(int64_t n_t, int64_t n_sig, const double* f, int64_t n_g, const
   if (rc) return rc;
   FTRY(cudaMemcpy(h, d_h.p, (size_t)n_t * n_sig * sizeof(double), cudaMemcpyDeviceToHost));
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_fmc_gather_device(int64_t q, int64_t n_t, int64_t R, const double* d_hist, int64_t n_pairs,
                           const int64_t* pair_tx, const int64_t* rx_ptr, const int64_t* rx_slot,
                           const double* rx_w, int64_t n_g, const double* in_sig, double* d_time_data,
-                          void* stream) {
+                          void* stream) try {
   bfe::set_last_error("");
   if (q <= 0 || n_t <= 0 || R <= 0 || n_pairs < 0 || n_g < 0) return ffail(BFE_ERR_ARG, "invalid sizes");
   if (n_pairs == 0) return BFE_OK;
@@ -193,11 +195,13 @@ int bfe_fmc_gather_device(int64_t q, int64_t n_t, int64_t R, const double* d_his
   if (conv) return launch_convolve(n_t, n_pairs, d_raw.p, in_sig, n_g, d_time_data, st);
   FTRY(cudaStreamSynchronize(st));
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_fmc_gather(int64_t q, int64_t n_t, int64_t R, const double* hist, int64_t n_pairs,
                    const int64_t* pair_tx, const int64_t* rx_ptr, const int64_t* rx_slot, const double* rx_w,
-                   int64_t n_g, const double* in_sig, double* time_data) {
+                   int64_t n_g, const double* in_sig, double* time_data) try {
   bfe::set_last_error("");
   if (q <= 0 || n_t <= 0 || R <= 0 || n_pairs < 0) return ffail(BFE_ERR_ARG, "invalid sizes");
   if (!hist || !time_data) return ffail(BFE_ERR_ARG, "NULL argument");
@@ -215,11 +219,13 @@ int bfe_fmc_gather(int64_t q, int64_t n_t, int64_t R, const double* hist, int64_
   if (rc) return rc;
   FTRY(cudaMemcpy(time_data, d_out.p, (size_t)n_t * n_pairs * sizeof(double), cudaMemcpyDeviceToHost));
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_disps_to_forces(const bfe_sparse* K, const bfe_sparse* C, const bfe_sparse* M, double dt, int64_t n_t,
                         const double* disp, const int32_t* lyrs, int32_t in_or_out, int32_t solver_mode,
-                        int64_t* n_force, int64_t* force_rows, double* force) {
+                        int64_t* n_force, int64_t* force_rows, double* force) try {
   bfe::set_last_error("");
   if (!K || !C || !M || !disp || !lyrs || !n_force || !force_rows) return ffail(BFE_ERR_ARG, "NULL argument");
   if (!(dt > 0) || n_t <= 0) return ffail(BFE_ERR_ARG, "invalid dt or n_t");
@@ -298,6 +304,8 @@ int bfe_disps_to_forces(const bfe_sparse* K, const bfe_sparse* C, const bfe_spar
   FTRY(cudaStreamSynchronize(st));
   FTRY(cudaMemcpy(force, d_out.p, rows.size() * (size_t)n_t * sizeof(double), cudaMemcpyDeviceToHost));
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 }  // extern "C"

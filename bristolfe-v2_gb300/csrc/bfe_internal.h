@@ -262,6 +262,12 @@ cudaError_t launch_grad_rho(const GradArgs& g, int precision, cudaStream_t s);
 // Message returned by bfe_last_error() on the calling thread.
 void set_last_error(const char* msg);
 
+// Status for the exception being handled (call it from a catch block): host
+// allocation failures give BFE_ERR_OOM, anything else BFE_ERR_ARG with the
+// exception's message. The C ABI entry points end in catch (...) blocks that
+// return it, so no exception crosses the boundary.
+int exception_status() noexcept;
+
 // Number of SMs of the current device (queried once per device, thread-safe).
 inline int sm_count() {
   static std::atomic<int> cache[64];

@@ -13,7 +13,9 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <new>
 #include <numeric>
+#include <stdexcept>
 #include <string>
 #include <thread>
 #include <vector>
@@ -293,6 +295,20 @@ struct DevBuf {
 }  // namespace
 
 void bfe::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
+int bfe::exception_status() noexcept {
+  try {
+    throw;
+  } catch (const std::bad_alloc&) {
+    return fail(BFE_ERR_OOM, "host memory allocation failed");
+  } catch (const std::length_error&) {
+    return fail(BFE_ERR_OOM, "host array too large");
+  } catch (const std::exception& e) {
+    return fail(BFE_ERR_ARG, "internal error: %s", e.what());
+  } catch (...) {
+    return fail(BFE_ERR_ARG, "internal error");
+  }
+}
 
 struct bfe_plan {
   int64_t n = 0;
@@ -1054,7 +1070,7 @@ extern "C" {
 
 int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse* Mv,
                        double dt, int32_t solver_mode, int32_t precision,
-                       const int64_t* dof_node, const int32_t* dof_type, uint32_t flags, bfe_plan** out) {
+                       const int64_t* dof_node, const int32_t* dof_type, uint32_t flags, bfe_plan** out) try {
   g_last_error.clear();
   if (!out) return fail(BFE_ERR_ARG, "out is NULL");
   *out = nullptr;
@@ -1065,10 +1081,12 @@ int bfe_plan_create_ex(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_spa
   if ((rc = to_csr(Mv, "M", M))) return rc;
   return create_plan(std::move(K), std::move(C), std::move(M), dt, solver_mode, precision, dof_node, dof_type,
                      flags, out);
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_plan_create_assembled(const bfe_matrices* mats, double dt, int32_t solver_mode, int32_t precision,
-                              bfe_plan** out) {
+                              bfe_plan** out) try {
   g_last_error.clear();
   if (!mats || !out) return fail(BFE_ERR_ARG, "NULL argument");
   int64_t n = 0, nnz[3] = {0, 0, 0}, n_nodes = 0;
@@ -1095,12 +1113,14 @@ int bfe_plan_create_assembled(const bfe_matrices* mats, double dt, int32_t solve
       if (g > 0) { dof_node[g - 1] = a; dof_type[g - 1] = d + 1; }
     }
   return bfe_plan_create(&v[0], &v[1], &v[2], dt, solver_mode, precision, dof_node.data(), dof_type.data(), out);
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_plan_create_multi(int32_t n_models, const bfe_sparse* K, const bfe_sparse* C,
                           const bfe_sparse* M, double dt, int32_t solver_mode, int32_t precision,
                           const int64_t* const* dof_node, const int32_t* const* dof_type,
-                          int64_t* row_offsets, bfe_plan** out) {
+                          int64_t* row_offsets, bfe_plan** out) try {
   g_last_error.clear();
   if (n_models < 1 || !K || !C || !M || !row_offsets || !out)
     return fail(BFE_ERR_ARG, "invalid arguments to bfe_plan_create_multi");
@@ -1161,6 +1181,8 @@ int bfe_plan_create_multi(int32_t n_models, const bfe_sparse* K, const bfe_spars
   *out = nullptr;
   return create_plan(std::move(Kj), std::move(Cj), std::move(Mj), dt, solver_mode, precision,
                      have ? node.data() : nullptr, have ? type.data() : nullptr, 0, out);
+} catch (...) {
+  return bfe::exception_status();
 }
 
 }  // extern "C"
@@ -1674,7 +1696,7 @@ extern "C" {
 
 int bfe_run_batched(bfe_plan* plan, int64_t R, int64_t n_t, const double* time,
                     int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
-                    int64_t q, const int64_t* hist_idx, double* hist_out) {
+                    int64_t q, const int64_t* hist_idx, double* hist_out) try {
   g_last_error.clear();
   if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
   if (R < 1) return fail(BFE_ERR_ARG, "R must be >= 1");
@@ -1719,12 +1741,14 @@ int bfe_run_batched(bfe_plan* plan, int64_t R, int64_t n_t, const double* time,
   }
   if (dev != plan->device) cudaSetDevice(dev);
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_run(bfe_plan* plan, int64_t n_t, const double* time,
             int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
             int64_t q, const int64_t* hist_idx, int64_t every_n, int32_t field_is_vel,
-            double* hist_out, double* fld_out, double* fld_time_out) {
+            double* hist_out, double* fld_out, double* fld_time_out) try {
   g_last_error.clear();
   if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
   if (every_n <= 0) {
@@ -1732,12 +1756,14 @@ int bfe_run(bfe_plan* plan, int64_t n_t, const double* time,
   }
   return run_one(plan, nullptr, n_t, time, p, frc_idx, frc_rows, frcs, q, hist_idx, every_n,
                  field_is_vel, hist_out, fld_out, fld_time_out);
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_run_field(bfe_plan* plan, const bfe_field* field, int64_t n_t, const double* time,
                   int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
                   int64_t q, const int64_t* hist_idx, int64_t every_n, int32_t field_is_vel,
-                  double* hist_out, double* el_out, double* fld_time_out) {
+                  double* hist_out, double* el_out, double* fld_time_out) try {
   g_last_error.clear();
   if (!plan || !field) return fail(BFE_ERR_ARG, "plan or field is NULL");
   if (bfe::field_ndof(field) != plan->n) return fail(BFE_ERR_ARG, "the field was created for a different number of DOFs");
@@ -1747,13 +1773,15 @@ int bfe_run_field(bfe_plan* plan, const bfe_field* field, int64_t n_t, const dou
   }
   return run_one(plan, field, n_t, time, p, frc_idx, frc_rows, frcs, q, hist_idx, every_n,
                  field_is_vel, hist_out, el_out, fld_time_out);
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,
                int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
                int64_t r, const int64_t* dsp_idx, int64_t dsp_rows, const double* dsps,
                int64_t q, const int64_t* hist_idx, int64_t every_n,
-               double* hist_out, double* fld_out, double* fld_time_out, double* frc_out) {
+               double* hist_out, double* fld_out, double* fld_time_out, double* frc_out) try {
   g_last_error.clear();
   if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
   if (plan->mode != BFE_MODE_V5) return fail(BFE_ERR_ARG, "the plan was not created with BFE_MODE_V5");
@@ -1970,13 +1998,15 @@ int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,
   if (n_frames) std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
   if (dev != plan->device) cudaSetDevice(dev);
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
                    int64_t n_frc, const int64_t* frc_dof, const int64_t* frc_rhs,
                    const int64_t* frc_sig, const double* frc_w,
                    int64_t n_sig, const double* d_sig,
-                   int64_t q, const int64_t* hist_idx, double* d_hist, void* stream) {
+                   int64_t q, const int64_t* hist_idx, double* d_hist, void* stream) try {
   g_last_error.clear();
   if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
   if (R < 1 || n_t < 1 || ti_start < 0 || n_frc < 0 || n_sig < 0 || q < 0)
@@ -2005,6 +2035,8 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
   rs.d_sig64 = d_sig;
   rs.d_hist = d_hist;
   return execute(plan, rs, static_cast<cudaStream_t>(stream));
+} catch (...) {
+  return bfe::exception_status();
 }
 
 // Adjoint gradient of an A-scan misfit with sqrt(N)-step checkpointing (see
@@ -2023,7 +2055,7 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
                          int64_t p, const int64_t* frc_idx, int64_t frc_rows, const double* frcs,
                          int64_t q, const int64_t* hist_idx, const double* observed,
                          int64_t ckpt_every, double* misfit, double* g_stiff, double* g_rho,
-                         double* hist_out) {
+                         double* hist_out) try {
   g_last_error.clear();
   if (!pl) return fail(BFE_ERR_ARG, "plan is NULL");
   if (pl->mode != BFE_MODE_VEL_CURRENT)
@@ -2228,6 +2260,8 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   CUDA_TRY(cudaStreamSynchronize(st));
   if (dev != pl->device) cudaSetDevice(dev);
   return BFE_OK;
+} catch (...) {
+  return bfe::exception_status();
 }
 
 }  // extern "C"
