@@ -126,3 +126,38 @@ def test_one_source_plan(bfe, plate, prec):
     for r in (0, 63):
         h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
         assert _err(hb[:, :, r], h0) <= TOL[prec], r
+
+
+def test_two_plans_used_concurrently_from_two_threads(bfe, plate):
+    """Distinct plans may run at the same time on different host threads
+    (the ABI's threading contract): an FP32 64-source run and an FP64
+    one-source run started together give the results they give alone."""
+    import threading
+    m = plate
+    t, s = modelgen.pulse(300, m["dt"])
+    nds = m["mon_nds"]
+    fi = modelgen.gi_of(m["gl"], [m["frc_nd"]], 2)
+    hi = modelgen.gi_of(m["gl"], nds, 2)
+    srcs = [modelgen.gi_of(m["gl"], [nds[r % nds.size]], 1 + r % 2) for r in range(64)]
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, "single", m["gl"]) as p32, \
+            bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, "double") as p64:
+        alone32 = p32.run_batched(t, srcs, s, hi)
+        alone64, _, _ = p64.run(t, fi, s, hi)
+        out, errors = {}, []
+
+        def work(name, fn):
+            try:
+                for k in range(3):
+                    out[(name, k)] = fn()
+            except Exception as e:          # reported below, on the test's thread
+                errors.append(e)
+        th = [threading.Thread(target=work, args=("f32", lambda: p32.run_batched(t, srcs, s, hi))),
+              threading.Thread(target=work, args=("f64", lambda: p64.run(t, fi, s, hi)[0]))]
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+    assert not errors, errors
+    for k in range(3):
+        assert np.array_equal(out[("f64", k)], alone64)
+        assert _err(out[("f32", k)], alone32) <= 1e-6
