@@ -1396,10 +1396,9 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   }
   auto launch_batched = [&](const bfe::NodeArgs* gpp, const bfe::GroupArgs* grpp, int v, int ib_n,
                             int ib_prev) -> cudaError_t {
-    if (v == 15 || v == 23) {
+    if (v == 15) {
       if (!grpp || !have_tmaps) return cudaErrorNotSupported;
-      return v == 15 ? bfe::launch_step_tma(a, *grpp, pl->tma, &tmaps[ib_n], &tmaps[ib_prev], st)
-                     : bfe::launch_step_tma_ws(a, *grpp, pl->tma, &tmaps[ib_n], &tmaps[ib_prev], st);
+      return bfe::launch_step_tma(a, *grpp, pl->tma, &tmaps[ib_n], &tmaps[ib_prev], st);
     }
     return bfe::launch_step_batched(a, gpp, grpp, prec, pl->max_slice_entries, v, st);
   };
@@ -1425,7 +1424,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       CUDA_TRY(cudaEventCreate(&e1));
       float best = 1e30f;
       for (int v = 0; v < nv; ++v) {
-        if ((v == 15 || v == 23) && !have_tmaps) continue;
+        if (v == 15 && !have_tmaps) continue;
         if (!bfe::batched_variant_supported(prec, (int)R, v, pl->have_node_blocks, pl->have_groups)) continue;
         CUDA_TRY(launch_batched(gp, grp, v, 1, 0));   // warm
         CUDA_TRY(cudaEventRecord(e0, st));
@@ -2128,9 +2127,9 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   int variant = !use_groups ? 0 : prec == BFE_PREC_SINGLE ? 20 : (R % 64 == 0 ? 1 : R % 32 == 0 ? 2 : 3);
   if (use_groups) {
     auto it = pl->variant_of_R.find(R);
-    // the TMA variants need tensor maps of the march's state buffers, which
-    // the adjoint's slot buffers do not have: they take the default kernel
-    if (it != pl->variant_of_R.end() && it->second != 15 && it->second != 23) variant = it->second;
+    // the TMA variant needs tensor maps of the march's state buffers, which
+    // the adjoint's slot buffers do not have: it takes the default kernel
+    if (it != pl->variant_of_R.end() && it->second != 15) variant = it->second;
   }
   auto step = [&](bfe::StepArgs& a) -> int {
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
