@@ -85,3 +85,41 @@ def test_disps_to_forces_matches_oracle(bfe, mode, in_or_out):
         assert np.array_equal(a, b)
     assert got[0].shape == ref[0].shape
     assert _err(got[0], ref[0]) <= 1e-12
+
+
+@pytest.mark.parametrize("mode", [VEL_CURRENT, VEL_LAST_HALF])
+@pytest.mark.parametrize("in_or_out", ["in", "out"])
+def test_subdomain_forces_reproduce_the_field(bfe, mode, in_or_out):
+    """The sub-domain principle end to end on the GPU: march a source, turn
+    the displacement history into forces on layers 2 and 3
+    (fn_convert_disps_to_forces_v2) with the frozen side zeroed, march those
+    forces alone, and the field is reproduced on the kept side (layers 1-2
+    for 'in', 3-4 for 'out') and zero on the frozen side. Layers are
+    one-node-wide bands in x; the source sits on the frozen side."""
+    m = modelgen.solid_plate(W=4e-3, H=2e-3, h=0.1e-3, dof_to_use=(1, 2), abs_thick=0.6e-3)
+    n = m["K"].shape[0]
+    gl = m["gl"]
+    nds = m["mod"]["nds"]
+    node_of = np.zeros(n, np.int64)
+    for d in range(gl.shape[1]):
+        ok = gl[:, d] > 0
+        node_of[gl[ok, d] - 1] = np.nonzero(ok)[0]
+    col = np.rint(nds[node_of, 0] / 0.1e-3).astype(int)          # node column of every DOF
+    lyrs = np.select([col < 17, col == 17, col == 18], [4, 3, 2], 1)
+    top = np.nonzero(np.isclose(nds[:, 1], nds[:, 1].max()))[0]
+    src_x = 0.9e-3 if in_or_out == "in" else 3.0e-3               # frozen side
+    src = top[np.argmin(np.abs(nds[top, 0] - src_x))] + 1
+    fi = modelgen.gi_of(gl, [src], 2)
+    nt = 260
+    t, s = modelgen.pulse(nt, m["dt"])
+    every = np.arange(1, n + 1)
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], mode, "double") as plan:
+        U, _, _ = plan.run(t, fi, s, every)                          # all DOFs, n x n_t
+        F, fset, _, _ = bfe.fn_convert_disps_to_forces_v2_gb300(m["K"], m["C"], m["M"], m["dt"], U, lyrs,
+                                                                 in_or_out, mode)
+        V, _, _ = plan.run(t, np.nonzero(fset)[0] + 1, F, every)
+    kept = (lyrs <= 2) if in_or_out == "in" else (lyrs >= 3)
+    scale = np.abs(U).max()
+    assert np.abs(U[kept]).max() > 1e-3 * scale                      # the wave reaches the kept side
+    assert np.abs(V[kept] - U[kept]).max() <= 1e-9 * scale
+    assert np.abs(V[~kept]).max() <= 1e-9 * scale

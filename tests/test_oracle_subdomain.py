@@ -67,3 +67,39 @@ def test_parse_to_fmc_sums_or_weights_the_receiver_rows():
     assert np.allclose(out[:, 0], dsps[0][5:8].T @ np.array([0.5, 1.0, 2.0]))
     assert np.allclose(out[:, 1], dsps[1][0:2].sum(axis=0))
     assert np.allclose(out[:, 2], dsps[2][9])
+
+
+@pytest.mark.parametrize("in_or_out", ["in", "out"])
+def test_oracle_subdomain_forces_reproduce_the_field(in_or_out):
+    """The sub-domain principle on the oracle: forces on layers 2 and 3 made
+    from a march's displacement history (frozen side zeroed) reproduce that
+    history on the kept side and nothing on the frozen side, to rounding."""
+    import modelgen
+    from oracle import solver as osolver
+    m = modelgen.solid_plate(W=3e-3, H=1.5e-3, h=0.1e-3, dof_to_use=(1, 2), abs_thick=0.4e-3)
+    n = m["K"].shape[0]
+    gl = m["gl"]
+    nds = m["mod"]["nds"]
+    node_of = np.zeros(n, np.int64)
+    for d in range(gl.shape[1]):
+        ok = gl[:, d] > 0
+        node_of[gl[ok, d] - 1] = np.nonzero(ok)[0]
+    col = np.rint(nds[node_of, 0] / 0.1e-3).astype(int)
+    lyrs = np.select([col < 12, col == 12, col == 13], [4, 3, 2], 1)
+    top = np.nonzero(np.isclose(nds[:, 1], nds[:, 1].max()))[0]
+    src = top[np.argmin(np.abs(nds[top, 0] - (0.6e-3 if in_or_out == "in" else 2.3e-3)))] + 1
+    fi = np.array([gl[src - 1, 1]])
+    t = np.arange(180) * m["dt"]
+    s = np.sin(2 * np.pi * 5e6 * t) * np.hanning(t.size)
+    every = np.arange(1, n + 1)
+    U = osolver.explicit_dynamic_solver_v6(m["K"], m["C"], m["M"], t, fi, s, [], [], every, np.inf, 0, "KE",
+                                           osolver.VEL_CURRENT)[0]
+    F, fset, _, _ = subdomain.convert_disps_to_forces_v2(m["K"], m["C"], m["M"], m["dt"], U, lyrs, in_or_out,
+                                                         osolver.VEL_CURRENT)
+    V = osolver.explicit_dynamic_solver_v6(m["K"], m["C"], m["M"], t, np.nonzero(fset)[0] + 1, F, [], [], every,
+                                           np.inf, 0, "KE", osolver.VEL_CURRENT)[0]
+    kept = (lyrs <= 2) if in_or_out == "in" else (lyrs >= 3)
+    scale = np.abs(U).max()
+    assert np.abs(U[kept]).max() > 1e-3 * scale
+    assert np.abs(V[kept] - U[kept]).max() <= 1e-12 * scale
+    assert np.abs(V[~kept]).max() <= 1e-12 * scale
