@@ -386,10 +386,15 @@ def run_ours(args):
 
     # end to end through the C ABI with host buffers (H2D signals, D2H A-scans)
     e2e_steps = 1
+    barrier()
     th0 = time.perf_counter()
     for _ in range(e2e_steps):
         plan32.run_batched(t, srcs, sig, mons)
     e2e_s = (time.perf_counter() - th0) / e2e_steps
+    if dist is not None:                      # the slowest rank, as for the device-timed value
+        te = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e_s = float(te.item())
     e2e_value = world * R * n * steps_per_march / e2e_s
     h2d = 8 * n_t * R + 8 * (p_max * R + q)
     d2h = 8 * q * n_t * R
