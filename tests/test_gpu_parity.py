@@ -277,3 +277,24 @@ def test_graph_replay_equals_plain_launches(bfe, coupled, prec, monkeypatch):
         monkeypatch.setenv("BFE_NO_GRAPH", "1")
         hp = plan.run_batched(t, srcs, s, hi)
     assert np.array_equal(hg, hp)
+
+
+@pytest.mark.parametrize("prec,tol", [("double", TOL64), ("single", TOL32)])
+def test_128_sources_take_two_chunks_per_lane(bfe, coupled, prec, tol):
+    """R = 128: the batched kernels loop over two 64-source chunks per lane
+    (FP32 half-warp kernels, FP64 group kernels); sources from both chunks
+    match the oracle."""
+    m = coupled
+    nt = 150
+    t, s = modelgen.pulse(nt, m["dt"])
+    nds = np.nonzero(m["gl"][:, 3] > 0)[0] + 1
+    R = 128
+    srcs = [modelgen.gi_of(m["gl"], [nds[(5 * r) % nds.size]], 4) for r in range(R)]
+    hi = np.concatenate([modelgen.gi_of(m["gl"], m["mon_nds"], 4), modelgen.gi_of(m["gl"], m["mon_nds"], 2)])
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], osolver.VEL_CURRENT, prec, m["gl"]) as plan:
+        hb = plan.run_batched(t, srcs, s, hi)
+        st = plan.stats()
+    assert st["n_groups"] == 2
+    for r in (0, 63, 64, 127):
+        h0, _, _, _ = _oracle(m, t, srcs[r], s, hi)
+        assert _err(hb[:, :, r], h0) <= tol, r
