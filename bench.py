@@ -686,21 +686,24 @@ def cpu_baseline(K, C, M, dt, t, src_gi, sig, mons, target_s=10.0):
 def _ref_subdomain(args):
     """Worker: one steel sub-domain model (square with absorbing layers on
     every side and a seeded void blob) built with the oracle's restatements
-    of the reference's mesh and assembly code; returns (K, C, M, dt)."""
+    of the reference's mesh and assembly code; returns (K, C, M, dt). The
+    geometry is our arm's (same void polygon for the seed, absorbers
+    min(3 wavelengths, side / 4) thick, quadratic grading), so both arms march
+    the same matrices."""
     from oracle import assembly, mesh, signals
     side, seed, h, fc = args
     steel = dict(rho=8000.0, D=signals.isotropic_stiffness_matrix(210e9, 0.3), el_typ="CPE3")
     mod = mesh.rectangular_structured_mesh(np.array([[0, 0], [side, 0], [side, side], [0, side]]), h)
-    rng = np.random.default_rng(seed)
-    blob = mesh.create_smooth_random_blob(0.5, 4, 64, rng) * (side / 10) + np.array([side / 2, side / 2])
+    blob = blob_polygon(min(1.5e-3, side / 8), (side / 2, side / 2), seed)
     mod = mesh.remove_elements_in_region(mod, blob)
     cL = np.sqrt(steel["D"][0, 0] / steel["rho"])
-    th = 3.0 * cL / fc
+    th = min(3.0 * cL / fc, side / 4)
     inner = np.array([[th, th], [side - th, th], [side - th, side - th], [th, side - th]])
     mod = mesh.add_absorbing_layer(mod, inner, th)
     mod["el_typ_i"] = ["CPE3"] * len(mod["el_mat_i"])
     K, C, M, _ = assembly.build_global_matrices_v5(mod["nds"], mod["els"], mod["el_mat_i"], mod["el_abs_i"],
-                                                   mod["el_typ_i"], [steel], dict(dof_to_use=[1, 2]))
+                                                   mod["el_typ_i"], [steel],
+                                                   dict(dof_to_use=[1, 2], damping_power_law=2))
     dt = signals.element_eigen_time_step(mod["nds"], mod["els"], steel["D"], steel["rho"])
     return K, C, M, dt
 
