@@ -54,3 +54,19 @@ def test_coupled_model_matches_the_reference_pipeline():
                                                     dict(dof_to_use=[1, 2, 4], damping_power_law=2))
     assert _same(K, m["K"]) and _same(C, m["C"]) and _same(M, m["M"])
     assert np.array_equal(np.asarray(gl), np.asarray(m["gl"]))
+
+
+def test_plate_matches_the_reference_pipeline_and_time_step():
+    """The C0 plate (DOFs 1-2 and the default 1-3): same K, C, M and
+    gl_lookup, and the same element-eigenvalue time step."""
+    W, H, h = 3e-3, 1.5e-3, 0.1e-3
+    for dofs in ((1, 2), (1, 2, 3)):
+        m = model.steel_plate(W=W, H=H, h=h, n_mon=4, dof_to_use=dofs)
+        mod = mesh.rectangular_structured_mesh(np.array([[0, 0], [W, 0], [W, H], [0, H]]), h)
+        mod["el_typ_i"] = ["CPE3"] * len(mod["el_mat_i"])
+        K, C, M, gl = assembly.build_global_matrices_v5(mod["nds"], mod["els"], mod["el_mat_i"], mod["el_abs_i"],
+                                                        mod["el_typ_i"], [STEEL], dict(dof_to_use=list(dofs)))
+        assert _same(K, m["K"]) and _same(M, m["M"]) and abs(C).sum() == abs(m["C"]).sum() == 0
+        assert np.array_equal(np.asarray(gl), np.asarray(m["gl"]))
+        dt = signals.element_eigen_time_step(mod["nds"], mod["els"], STEEL["D"], STEEL["rho"])
+        assert abs(dt - m["dt"]) <= 1e-12 * dt
