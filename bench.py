@@ -47,7 +47,8 @@ def parse():
                     help="shrink the model size (testing only; 1.0 = the benchmark model)")
     ap.add_argument("--n-t", type=int, default=None)
     ap.add_argument("--no-extra", action="store_true",
-                    help="skip the 3D and adjoint sections (quick runs)")
+                    help="skip the extra sections (C0 plate, FMC, assembly, 3D, adjoint); runs with "
+                         "more than one GPU always skip them")
     ap.add_argument("--subdomains", type=int, default=32,
                     help="steel sub-domain models marched with the coupled model (32 = benchmark)")
     ap.add_argument("--only", choices=["adjoint"], default=None,
@@ -400,7 +401,9 @@ def run_ours(args):
     d2h = 8 * q * n_t * R
 
     extra = {}
-    if rank == 0 and not args.no_extra:
+    # the extra sections run in one-GPU runs only: under torchrun the other
+    # ranks would hold their GPUs idle in the final barrier meanwhile
+    if rank == 0 and world == 1 and not args.no_extra:
         extra["plate_c0"] = plate_c0_section(bfe_gb300, model)
         extra["fmc_c2a"] = fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, mon_parts[0].size, sig, stream)
         extra["assembly_c1"] = assembly_section(torch, bfe_gb300, model, main)
