@@ -51,7 +51,7 @@ def parse():
                          "more than one GPU always skip them")
     ap.add_argument("--subdomains", type=int, default=32,
                     help="steel sub-domain models marched with the coupled model (32 = benchmark)")
-    ap.add_argument("--only", choices=["adjoint"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "c1"], default=None,
                     help="run one extra section alone and print its JSON (profiling); --n-t sets its "
                          "samples, finite-difference checks are skipped")
     return ap.parse_args()
@@ -405,6 +405,7 @@ def run_ours(args):
     # ranks would hold their GPUs idle in the final barrier meanwhile
     if rank == 0 and world == 1 and not args.no_extra:
         extra["plate_c0"] = plate_c0_section(bfe_gb300, model)
+        extra["coupled_c1"] = coupled_c1_section(torch, bfe_gb300, model, main, peak)
         extra["fmc_c2a"] = fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, mon_parts[0].size, sig, stream)
         extra["assembly_c1"] = assembly_section(torch, bfe_gb300, model, main)
         extra["hex3d_c3"] = hex3d_section(torch, bfe_gb300, model)
@@ -497,6 +498,45 @@ def plate_c0_section(bfe_gb300, model):
     _, s = cpu_port.time_march(op, t, fi - 1, sig[None, :], hi - 1)
     res["cpu_port"] = {"s": s, "dof_updates_per_s": m["K"].shape[0] * n_t / s, "threads": cpu_port.threads()}
     res["speedup_fp64_call_vs_cpu"] = s / res["double"]["call_s"]
+    return res
+
+
+def coupled_c1_section(torch, bfe_gb300, model, main, peak, n_t=8000):
+    """The coupled water/steel model on its own with one source (the array's
+    centre element, pressure DOF), 8,000 samples, the 64 element centres
+    monitored: one-source marches on resident FP64 and FP32 plans (host
+    buffers), FP32 A-scans against FP64, and the step kernels' average launch
+    (CUDA events) against the HBM roofline (R = 1 bytes)."""
+    m = main
+    n = int(m["K"].shape[0])
+    t = np.arange(n_t) * m["dt"]
+    sig = model.toneburst(t, 5e6, 5)
+    fi = model.global_indices(m["gl"], m["src_nodes"][len(m["src_nodes"]) // 2], 4)
+    hi = model.global_indices(m["gl"], m["mon_nodes"], 4)
+    res = {"n_dof": n, "nnz_K": int(m["K"].nnz), "samples": n_t, "source_dofs": int(fi.size),
+           "monitors": int(hi.size)}
+    h64 = None
+    for prec, b in (("double", 8), ("single", 4)):
+        with bfe_gb300.Plan(m["K"], m["C"], m["M"], m["dt"], bfe_gb300.VEL_CURRENT, prec,
+                            m["gl"] if prec == "single" else None, one_source=True) as plan:
+            plan.run(t[:200], fi, sig[:200], hi)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h, _, _ = plan.run(t, fi, sig, hi)
+            el = time.perf_counter() - t0
+            plan.set_timing(True)
+            plan.run(t, fi, sig, hi)
+            st = plan.stats()
+            plan.set_timing(False)
+        ms = st["step_ms"] / max(st["step_launches"], 1)
+        by = algorithmic_bytes(m["K"].nnz, n, 1, fi.size, hi.size, b)
+        res[prec] = {"march_s": el, "dof_updates_per_s": n * n_t / el, "step_kernel_ms": ms,
+                     "achieved_gbs": by / ms / 1e6, "frac_of_measured_hbm": by / ms / 1e6 / peak,
+                     "state_mb": 3 * n * b / 1e6}
+        if prec == "double":
+            h64 = h
+        else:
+            res[prec]["ascan_err_vs_fp64"] = float(np.abs(h - h64).max() / np.abs(h64).max())
     return res
 
 
@@ -806,6 +846,14 @@ def run_only(args):
     from bfe_gb300 import model
     torch.cuda.set_device(0)
     bfe_gb300.load()
+    if args.only == "c1":
+        w = workload(1.0)
+        main = model.coupled_water_steel(W=w["W"], H_water=w["H_water"], H_steel=w["H_steel"], h=w["h"],
+                                         fc=w["fc"], blob_polygon_pts=w["blob"], array_elements=w["n_src"],
+                                         array_pitch=w["pitch"])
+        res = coupled_c1_section(torch, bfe_gb300, model, main, measured_peak_hbm()[0], n_t=args.n_t or 8000)
+        print(json.dumps({"section": "coupled_c1", **res}), flush=True)
+        return
     res = adjoint_section(torch, bfe_gb300, model, n_fd=0, n_t=args.n_t or 4000)
     print(json.dumps({"section": "adjoint_c4", **res}), flush=True)
 
