@@ -155,6 +155,12 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
 size_t batched_smem_bytes(int precision, int max_slice_entries);
 cudaError_t set_batched_smem_limit(int precision, size_t smem);
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);
+// Group block-sparse kernel families (bfe_group_kernels.cu), by batched
+// variant: packed warp-per-node for block size maxbs (2 or 3), half-warp
+// float4 with lpn lanes per node (16, 8 or 4), FP64 direct form.
+cudaError_t launch_group2_variant(int maxbs, const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t s);
+cudaError_t launch_group4_variant(int lpn, const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t s);
+cudaError_t launch_group64_variant(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t s);
 cudaError_t launch_frame(const StepArgs& a, int precision, double* fld, int64_t frame,
                          int field_is_vel, double dt, cudaStream_t s);
 cudaError_t launch_cast_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);

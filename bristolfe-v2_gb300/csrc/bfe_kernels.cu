@@ -22,48 +22,10 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "bfe_device.cuh"
 #include "bfe_internal.h"
 
 namespace bfe {
-
-template <typename T> struct Vec2;
-template <> struct Vec2<float> { using type = float2; };
-template <> struct Vec2<double> { using type = double2; };
-
-__device__ __forceinline__ int lower_bound_i32(const int32_t* a, int n, int key) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (__ldg(a + mid) < key) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
-// Sum of coef * signal over the forcing entries of row i for right-hand side r.
-template <typename T>
-__device__ __forceinline__ T forcing_sum(const StepArgs& a, int i, int r) {
-  const T* coef = static_cast<const T*>(a.frc_coef);
-  const T* sig = static_cast<const T*>(a.sig) + (size_t)step_index(a) * a.n_sig;
-  T f = T(0);
-  for (int e = lower_bound_i32(a.frc_row, a.n_frc, i); e < a.n_frc && __ldg(a.frc_row + e) == i; ++e) {
-    if (__ldg(a.frc_rhs + e) == r) f += __ldg(coef + e) * __ldg(sig + __ldg(a.frc_sig + e));
-  }
-  return f;
-}
-
-__device__ __forceinline__ void write_history(const StepArgs& a, int i, int r, double v) {
-  for (int k = lower_bound_i32(a.mon_row, a.n_mon, i); k < a.n_mon && __ldg(a.mon_row + k) == i; ++k) {
-    int slot = __ldg(a.mon_slot + k);
-    a.hist[(size_t)slot + (size_t)a.q * ((size_t)step_index(a) + (size_t)a.n_t * r)] = v;
-  }
-}
-
-// Error-free transformation: s + e == a + b exactly (Knuth two-sum).
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
 
 // ---------------------------------------------------------------------------
 // FP64, one right-hand side: one thread per row.
@@ -761,417 +723,6 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, 2) step_f32_group_async(Step
 size_t async_smem_bytes() { return (size_t)kAsyncWarps * 2 * kStageFloats * sizeof(float); }
 
 // ---------------------------------------------------------------------------
-// FP32 group block-sparse kernel, packed-math form (R a multiple of 64).
-// One warp per node of a group, each lane owns two right-hand sides held as
-// a float2 and every arithmetic operation is one packed FP32x2 instruction
-// (__ffma2_rn / __fadd2_rn: IEEE round-to-nearest per component, the same
-// results as two scalar operations). Coefficients are stored as pre-broadcast
-// float2 pairs ({c, c}). The neighbour differences are formed as
-// (u_own - u_nbr), so the accumulator holds -Lp u and the compensated update
-// needs no negation.
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {        // a - b, exact rounding
-  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
-}
-__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
-  s = __fadd2_rn(a, b);
-  const float2 bb = f2sub(s, a);
-  e = __fadd2_rn(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
-}
-
-template <int BS, int UNROLL>
-__device__ __forceinline__ void group2_node(const StepArgs& a, const GroupArgs& gr, int gi,
-                                            int node, int lane) {
-  const int row0 = __ldg(gr.row0[gi] + node);
-  const int p0 = __ldg(gr.nptr[gi] + node), p1 = __ldg(gr.nptr[gi] + node + 1);
-  const int32_t* nrow = gr.nrow[gi];
-  const float2* coef = gr.coef2[gi];
-  const int R = a.R;
-  const size_t rstride = (size_t)R * sizeof(float);
-  for (int c = lane * 2; c < R; c += 64) {
-    const char* ub = reinterpret_cast<const char*>(static_cast<const float*>(a.u_n) + c);
-    float2 uo[BS], acc[BS];
-#pragma unroll
-    for (int k = 0; k < BS; ++k) {
-      uo[k] = __ldg(reinterpret_cast<const float2*>(ub + (size_t)(row0 + k) * rstride));
-      acc[k] = make_float2(0.f, 0.f);
-    }
-#pragma unroll UNROLL
-    for (int e = p0; e < p1; ++e) {
-      const char* nb = ub + (size_t)__ldg(nrow + e) * rstride;
-      const float2* cb = coef + (size_t)e * (BS * BS);
-#pragma unroll
-      for (int l = 0; l < BS; ++l) {
-        const float2 g = __ldg(reinterpret_cast<const float2*>(nb + l * rstride));
-        const float2 dn = f2sub(uo[l], g);                      // u_own - u_nbr
-#pragma unroll
-        for (int k = 0; k < BS; ++k) acc[k] = __ffma2_rn(__ldg(cb + k * BS + l), dn, acc[k]);
-      }
-    }
-    float* unew = static_cast<float*>(a.u_new);
-#pragma unroll
-    for (int k = 0; k < BS; ++k) {
-      const int row = row0 + k;
-      const uint32_t info = __ldg(a.rowinfo + row);
-      const float q = __ldg(static_cast<const float*>(a.rowc) + row);
-      const size_t o = (size_t)row * R + c;
-      const float2 up = __ldcs(reinterpret_cast<const float2*>(static_cast<const float*>(a.u_prev) + o));
-      float2 d, err;
-      two_sum2(uo[k], make_float2(-up.x, -up.y), d, err);
-      const float2 q2 = make_float2(q, q);
-      float2 inc = __ffma2_rn(q2, d, acc[k]);                    // q d - Lp u
-      if (info & kRowForced)
-        inc = __fadd2_rn(inc, make_float2(forcing_sum<float>(a, row, c), forcing_sum<float>(a, row, c + 1)));
-      inc = __ffma2_rn(q2, err, inc);
-      const float2 r = __fadd2_rn(uo[k], inc);
-      *reinterpret_cast<float2*>(unew + o) = r;
-      if (info & kRowInterface) {
-        const int t = lower_bound_i32(a.int_row, a.n_int, row);
-        const float2 vi = a.int_base_prev ? __fadd2_rn(__fadd2_rn(d, err), inc) : __fadd2_rn(d, err);
-        *reinterpret_cast<float2*>(static_cast<float*>(a.v_int) + (size_t)t * R + c) = vi;
-      } else if (info & kRowMonitored) {
-        write_history(a, row, c, (double)r.x);
-        write_history(a, row, c + 1, (double)r.y);
-      }
-    }
-  }
-}
-
-template <int MAXBS, int UNROLL, int MINB>
-__global__ void __launch_bounds__(256, MINB) step_f32_group2(StepArgs a, GroupArgs gr) {
-  const int lane = threadIdx.x & 31;
-  const int b = blockIdx.x;
-  int gi = 0;
-#pragma unroll
-  for (int k = 1; k < kMaxGroups; ++k)
-    if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
-  const int node = (b - gr.blk_begin[gi]) * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (node >= gr.n_nodes[gi]) return;
-  if (gr.bs[gi] == 1) group2_node<1, UNROLL * 2>(a, gr, gi, node, lane);
-  else if (MAXBS == 2 || gr.bs[gi] == 2) group2_node<(MAXBS >= 2 ? 2 : 1), UNROLL>(a, gr, gi, node, lane);
-  else group2_node<MAXBS, UNROLL>(a, gr, gi, node, lane);
-}
-
-// Group block-sparse kernel with a half-warp per node: each lane carries four
-// right-hand sides (float4), so every load, address and index instruction
-// serves two nodes, and a warp holds two nodes' work at the cost of one.
-// UNROLL neighbours are loaded before they are used; LATE_UP reads u_{n-1}
-// only in the epilogue (fewer live registers); RAW reads a 2 x 2 block's
-// coefficients with one 16-byte load of the plain [k][l] array and forms the
-// broadcast pairs in registers (half the coefficient bytes and loads).
-__device__ __forceinline__ float4 f4sub(float4 a, float4 b) {
-  const float2 lo = f2sub(make_float2(a.x, a.y), make_float2(b.x, b.y));
-  const float2 hi = f2sub(make_float2(a.z, a.w), make_float2(b.z, b.w));
-  return make_float4(lo.x, lo.y, hi.x, hi.y);
-}
-__device__ __forceinline__ float4 f4fma(float2 c, float4 x, float4 acc) {   // c.x == c.y
-  const float2 lo = __ffma2_rn(c, make_float2(x.x, x.y), make_float2(acc.x, acc.y));
-  const float2 hi = __ffma2_rn(c, make_float2(x.z, x.w), make_float2(acc.z, acc.w));
-  return make_float4(lo.x, lo.y, hi.x, hi.y);
-}
-
-// One neighbour block of a node: acc_k += sum_l c_kl (u_own_l - u_nbr_l).
-template <int BS, bool RAW>
-__device__ __forceinline__ void group4_nbr(const float* nb, const float2* coef, const float* craw, int e,
-                                           size_t rs, const float4 (&uo)[BS], float4 (&acc)[BS]) {
-  float4 g[BS];
-#pragma unroll
-  for (int l = 0; l < BS; ++l) g[l] = __ldg(reinterpret_cast<const float4*>(nb + l * rs));
-  float2 cv[BS * BS];
-  if (RAW && BS == 2) {
-    const float4 cr = __ldg(reinterpret_cast<const float4*>(craw + (size_t)e * 4));
-    cv[0] = make_float2(cr.x, cr.x);
-    cv[1] = make_float2(cr.y, cr.y);
-    cv[2 % (BS * BS)] = make_float2(cr.z, cr.z);
-    cv[3 % (BS * BS)] = make_float2(cr.w, cr.w);
-  } else if (RAW) {
-    const float cr = __ldg(craw + e);
-    cv[0] = make_float2(cr, cr);
-  } else if (BS == 2) {
-    const float4 c0 = __ldg(reinterpret_cast<const float4*>(coef + (size_t)e * 4));
-    const float4 c1 = __ldg(reinterpret_cast<const float4*>(coef + (size_t)e * 4 + 2));
-    cv[0] = make_float2(c0.x, c0.y);
-    cv[1] = make_float2(c0.z, c0.w);
-    cv[2 % (BS * BS)] = make_float2(c1.x, c1.y);
-    cv[3 % (BS * BS)] = make_float2(c1.z, c1.w);
-  } else {
-    cv[0] = __ldg(coef + e);
-  }
-#pragma unroll
-  for (int l = 0; l < BS; ++l) {
-    const float4 dn = f4sub(uo[l], g[l]);                     // u_own - u_nbr
-#pragma unroll
-    for (int k = 0; k < BS; ++k) acc[k] = f4fma(cv[k * BS + l], dn, acc[k]);
-  }
-}
-
-// Compensated update of four right-hand sides of one row (c .. c + 3):
-// u_new = u_n + q (u_n - u_{n-1}) - Lp u_n + forcing with the two-sum of
-// (u_n - u_{n-1}), interface staging and history as the other kernels.
-__device__ __forceinline__ void finish4(const StepArgs& a, int row, int c, float4 uo, float4 acc, float4 up) {
-  const uint32_t info = __ldg(a.rowinfo + row);
-  const float q = __ldg(static_cast<const float*>(a.rowc) + row);
-  const size_t o = (size_t)row * a.R + c;
-  const float2 q2 = make_float2(q, q);
-  float2 res[2], vin[2];
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const float2 u = h ? make_float2(uo.z, uo.w) : make_float2(uo.x, uo.y);
-    const float2 p = h ? make_float2(up.z, up.w) : make_float2(up.x, up.y);
-    const float2 ac = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
-    float2 d, err;
-    two_sum2(u, make_float2(-p.x, -p.y), d, err);
-    float2 inc = __ffma2_rn(q2, d, ac);                        // q d - Lp u
-    if (info & kRowForced)
-      inc = __fadd2_rn(inc, make_float2(forcing_sum<float>(a, row, c + 2 * h),
-                                        forcing_sum<float>(a, row, c + 2 * h + 1)));
-    inc = __ffma2_rn(q2, err, inc);
-    res[h] = __fadd2_rn(u, inc);
-    vin[h] = a.int_base_prev ? __fadd2_rn(__fadd2_rn(d, err), inc) : __fadd2_rn(d, err);
-  }
-  *reinterpret_cast<float4*>(static_cast<float*>(a.u_new) + o) = make_float4(res[0].x, res[0].y, res[1].x, res[1].y);
-  if (info & kRowInterface) {
-    const int t = lower_bound_i32(a.int_row, a.n_int, row);
-    *reinterpret_cast<float4*>(static_cast<float*>(a.v_int) + (size_t)t * a.R + c) =
-        make_float4(vin[0].x, vin[0].y, vin[1].x, vin[1].y);
-  } else if (info & kRowMonitored) {
-    write_history(a, row, c, (double)res[0].x);
-    write_history(a, row, c + 1, (double)res[0].y);
-    write_history(a, row, c + 2, (double)res[1].x);
-    write_history(a, row, c + 3, (double)res[1].y);
-  }
-}
-
-// One-DOF (fluid) node with 8 lanes: each lane carries the right-hand sides
-// c .. c + 3 and c + 32 .. c + 35, so a neighbour's index and coefficient
-// serve 512 bytes of state as in the two-DOF form.
-template <int UNROLL, bool RAW>
-__device__ __forceinline__ void group4_fluid(const StepArgs& a, const GroupArgs& gr, int gi, int node, int l8) {
-  const int4 rec = __ldg(gr.rec[gi] + node);
-  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
-  const int R = a.R;
-  const size_t rs = (size_t)R;
-  const float* un = static_cast<const float*>(a.u_n);
-  const int32_t* nrow = gr.nrow[gi];
-  const float2* coef = gr.coef2[gi];
-  const float* craw = gr.coef[gi];
-  for (int c = l8 * 4; c < R; c += 64) {
-    const float* own = un + (size_t)row0 * rs + c;
-    const float4 uo0 = __ldg(reinterpret_cast<const float4*>(own));
-    const float4 uo1 = __ldg(reinterpret_cast<const float4*>(own + 32));
-    float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
-#pragma unroll UNROLL
-    for (int e = p0; e < p1; ++e) {
-      const float* nb = un + (size_t)__ldg(nrow + e) * rs + c;
-      const float4 g0 = __ldg(reinterpret_cast<const float4*>(nb));
-      const float4 g1 = __ldg(reinterpret_cast<const float4*>(nb + 32));
-      float2 cv;
-      if (RAW) { const float cr = __ldg(craw + e); cv = make_float2(cr, cr); }
-      else cv = __ldg(coef + e);
-      acc0 = f4fma(cv, f4sub(uo0, g0), acc0);
-      acc1 = f4fma(cv, f4sub(uo1, g1), acc1);
-    }
-    const float* upv = static_cast<const float*>(a.u_prev) + (size_t)row0 * rs + c;
-    finish4(a, row0, c, uo0, acc0, __ldcs(reinterpret_cast<const float4*>(upv)));
-    finish4(a, row0, c + 32, uo1, acc1, __ldcs(reinterpret_cast<const float4*>(upv + 32)));
-  }
-}
-
-template <int BS, int UNROLL, bool LATE_UP, bool RAW, int LPN>
-__device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& gr, int gi, int node,
-                                            int l16) {
-  const int4 rec = __ldg(gr.rec[gi] + node);
-  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
-  const int R = a.R;
-  const size_t rs = (size_t)R;
-  const float* un = static_cast<const float*>(a.u_n);
-  const int32_t* nrow = gr.nrow[gi];
-  const float2* coef = gr.coef2[gi];
-  const float* craw = gr.coef[gi];
-  for (int c = l16 * 4; c < R; c += 4 * LPN) {
-    float4 uo[BS], up[BS], acc[BS];
-#pragma unroll
-    for (int k = 0; k < BS; ++k) {
-      uo[k] = __ldg(reinterpret_cast<const float4*>(un + (size_t)(row0 + k) * rs + c));
-      if (!LATE_UP)
-        up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) +
-                                                        (size_t)(row0 + k) * rs + c));
-      acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-#pragma unroll UNROLL
-    for (int e = p0; e < p1; ++e)
-      group4_nbr<BS, RAW>(un + (size_t)__ldg(nrow + e) * rs + c, coef, craw, e, rs, uo, acc);
-#pragma unroll
-    for (int k = 0; k < BS; ++k) {
-      const int row = row0 + k;
-      if (LATE_UP)
-        up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) + (size_t)row * rs + c));
-      finish4(a, row, c, uo[k], acc[k], up[k]);
-    }
-  }
-}
-
-// 128 threads = 128 / LPN nodes of LPN lanes each (LPN = 16 for R a
-// multiple of 64, 8 for R = 32, 4 for R = 16); gr.blk_begin must hold the
-// CTA ranges for 128 / LPN nodes per CTA.
-template <int UNROLL, int MINB, bool LATE_UP, bool RAW, int LPN = 16>
-__global__ void __launch_bounds__(128, MINB) step_f32_group4(StepArgs a, GroupArgs gr) {
-  const int b = blockIdx.x;
-  int gi = 0;
-#pragma unroll
-  for (int k = 1; k < kMaxGroups; ++k)
-    if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
-  if (LPN == 16 && gr.bs[gi] == 1) {                    // one-DOF nodes: 8 lanes, 16 nodes per CTA
-    const int node = (b - gr.blk_begin[gi]) * 16 + (threadIdx.x >> 3);
-    if (node >= gr.n_nodes[gi]) return;
-    group4_fluid<UNROLL, RAW>(a, gr, gi, node, threadIdx.x & 7);
-    return;
-  }
-  const int node = (b - gr.blk_begin[gi]) * (128 / LPN) + threadIdx.x / LPN;
-  if (node >= gr.n_nodes[gi]) return;
-  if (gr.bs[gi] == 1) group4_node<1, UNROLL * 2, LATE_UP, RAW, LPN>(a, gr, gi, node, threadIdx.x % LPN);
-  else group4_node<2, UNROLL, LATE_UP, RAW, LPN>(a, gr, gi, node, threadIdx.x % LPN);
-}
-
-// The variants of the half-warp family for lanes-per-node LPN.
-template <int LPN>
-static void launch_group4(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {
-  GroupArgs g = gr;
-  int blocks = 0;
-  for (int k = 0; k < g.n_groups; ++k) {
-    const int npc = (LPN == 16 && g.bs[k] == 1) ? 16 : 128 / LPN;     // nodes per CTA
-    g.blk_begin[k] = blocks;
-    blocks += (g.n_nodes[k] + npc - 1) / npc;
-  }
-  g.blk_begin[g.n_groups] = blocks;
-  switch (variant) {
-    case 16: step_f32_group4<1, 10, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 17: step_f32_group4<2, 8, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 18: step_f32_group4<1, 12, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 19: step_f32_group4<1, 12, true, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 20: step_f32_group4<1, 12, false, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 21: step_f32_group4<1, 12, true, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    default: step_f32_group4<1, 10, false, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-  }
-}
-
-// FP64 group block-sparse kernel (direct form, the reference's arithmetic):
-// u_new = sum over the node's blocks (its own included) of B_block u_n
-// + D u_{n-1} + forcing, summed in column order like the one-source kernel.
-// LPN lanes per node, VEC doubles (right-hand sides) per lane and pass.
-template <int BS, int LPN, int VEC>
-__device__ __forceinline__ void group64_node(const StepArgs& a, const GroupArgs& gr, int gi, int node,
-                                             int lane) {
-  const int4 rec = __ldg(gr.rec[gi] + node);
-  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
-  const int R = a.R;
-  const size_t rs = (size_t)R;
-  const double* un = static_cast<const double*>(a.u_n);
-  const int32_t* nrow = gr.nrow[gi];
-  const double* cf = gr.coef64[gi];
-  for (int c = lane * VEC; c < R; c += LPN * VEC) {
-    double acc[BS][VEC];
-#pragma unroll
-    for (int k = 0; k < BS; ++k)
-#pragma unroll
-      for (int v = 0; v < VEC; ++v) acc[k][v] = 0.0;
-    for (int e = p0; e < p1; ++e) {
-      const double* nb = un + (size_t)__ldg(nrow + e) * rs + c;
-      double g[BS][VEC];
-#pragma unroll
-      for (int l = 0; l < BS; ++l)
-#pragma unroll
-        for (int v = 0; v < VEC; v += 2) {
-          const double2 x = __ldg(reinterpret_cast<const double2*>(nb + l * rs + v));
-          g[l][v] = x.x;
-          g[l][v + 1] = x.y;
-        }
-      double cv[BS * BS];
-#pragma unroll
-      for (int t = 0; t < BS * BS; ++t) cv[t] = __ldg(cf + (size_t)e * (BS * BS) + t);
-#pragma unroll
-      for (int l = 0; l < BS; ++l)
-#pragma unroll
-        for (int k = 0; k < BS; ++k)
-#pragma unroll
-          for (int v = 0; v < VEC; ++v) acc[k][v] = fma(cv[k * BS + l], g[l][v], acc[k][v]);
-    }
-    double* unew = static_cast<double*>(a.u_new);
-    const double* upv = static_cast<const double*>(a.u_prev);
-#pragma unroll
-    for (int k = 0; k < BS; ++k) {
-      const int row = row0 + k;
-      const uint32_t info = __ldg(a.rowinfo + row);
-      const double dk = __ldg(static_cast<const double*>(a.rowc) + row);
-      const size_t o = (size_t)row * rs + c;
-      double res[VEC], upk[VEC];
-#pragma unroll
-      for (int v = 0; v < VEC; v += 2) {
-        const double2 x = __ldcs(reinterpret_cast<const double2*>(upv + o + v));
-        upk[v] = x.x;
-        upk[v + 1] = x.y;
-      }
-#pragma unroll
-      for (int v = 0; v < VEC; ++v) {
-        double r = acc[k][v] + dk * upk[v];
-        if (info & kRowForced) r += forcing_sum<double>(a, row, c + v);
-        res[v] = r;
-      }
-#pragma unroll
-      for (int v = 0; v < VEC; v += 2)
-        *reinterpret_cast<double2*>(unew + o + v) = make_double2(res[v], res[v + 1]);
-      if (info & kRowInterface) {
-        const int t = lower_bound_i32(a.int_row, a.n_int, row);
-        double* vi = static_cast<double*>(a.v_int) + (size_t)t * R + c;
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) vi[v] = a.int_base_prev ? (res[v] - upk[v]) : (un[o + v] - upk[v]);
-      } else if (info & kRowMonitored) {
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) write_history(a, row, c + v, res[v]);
-      }
-    }
-  }
-}
-
-template <int LPN, int VEC, int MINB, int MAXBS>
-__global__ void __launch_bounds__(128, MINB) step_f64_group(StepArgs a, GroupArgs gr) {
-  const int b = blockIdx.x;
-  int gi = 0;
-#pragma unroll
-  for (int k = 1; k < kMaxGroups; ++k)
-    if (k < gr.n_groups && b >= gr.blk_begin[k]) gi = k;
-  const int node = (b - gr.blk_begin[gi]) * (128 / LPN) + threadIdx.x / LPN;
-  if (node >= gr.n_nodes[gi]) return;
-  if (gr.bs[gi] == 1) group64_node<1, LPN, VEC>(a, gr, gi, node, threadIdx.x % LPN);
-  else if (MAXBS == 2 || gr.bs[gi] == 2) group64_node<(MAXBS >= 2 ? 2 : 1), LPN, VEC>(a, gr, gi, node, threadIdx.x % LPN);
-  else group64_node<MAXBS, LPN, VEC>(a, gr, gi, node, threadIdx.x % LPN);
-}
-
-// FP64 variants: 1 = 16 lanes x 4 right-hand sides (R a multiple of 64),
-// 2 = 16 x 2 (R a multiple of 32), 3 = 8 x 2 (R a multiple of 16).
-static cudaError_t launch_group64(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {
-  const int lpn = variant == 3 ? 8 : 16;
-  GroupArgs g = gr;
-  int blocks = 0;
-  for (int k = 0; k < g.n_groups; ++k) {
-    g.blk_begin[k] = blocks;
-    blocks += (g.n_nodes[k] + 128 / lpn - 1) / (128 / lpn);
-  }
-  g.blk_begin[g.n_groups] = blocks;
-  int maxbs = 1;
-  for (int k = 0; k < g.n_groups; ++k) maxbs = g.bs[k] > maxbs ? g.bs[k] : maxbs;
-  if (maxbs <= 2) {
-    if (variant == 1) step_f64_group<16, 4, 8, 2><<<blocks, 128, 0, st>>>(a, g);
-    else if (variant == 2) step_f64_group<16, 2, 10, 2><<<blocks, 128, 0, st>>>(a, g);
-    else step_f64_group<8, 2, 10, 2><<<blocks, 128, 0, st>>>(a, g);
-  } else {
-    if (variant == 1) step_f64_group<16, 4, 6, 3><<<blocks, 128, 0, st>>>(a, g);
-    else if (variant == 2) step_f64_group<16, 2, 8, 3><<<blocks, 128, 0, st>>>(a, g);
-    else step_f64_group<8, 2, 8, 3><<<blocks, 128, 0, st>>>(a, g);
-  }
-  return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
 // Interface correction: u_new[row] = base + sum_z Z[t, z] v[z], one thread
 // per (interface row, right-hand side).
 template <typename T>
@@ -1309,7 +860,7 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 }
 
 // Variants for the autotuner. FP64 with group arrays and R % 16 == 0: 0 =
-// slice-staged rows, 1-3 = the FP64 group kernel (launch_group64). FP32
+// slice-staged rows, 1-3 = the FP64 group kernel (launch_group64_variant). FP32
 // with R % 64 == 0: 0 = slice-staged
 // row kernel, 1..3 = half-warp float4 row kernels, 4 = node-block kernel
 // (only when the plan has node blocks), 5 = node-block kernel, deeper unroll.
@@ -1340,26 +891,13 @@ bool batched_variant_supported(int precision, int R, int variant, bool have_node
   return true;
 }
 
-template <int MAXBS>
-static void launch_group2(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {
-  const int grid = gr.blk_begin[gr.n_groups];
-  switch (variant) {
-    case 9: step_f32_group2<MAXBS, 1, 1><<<grid, 256, 0, st>>>(a, gr); break;
-    case 10: step_f32_group2<MAXBS, 2, 1><<<grid, 256, 0, st>>>(a, gr); break;
-    case 11: step_f32_group2<MAXBS, 4, 1><<<grid, 256, 0, st>>>(a, gr); break;
-    case 12: step_f32_group2<MAXBS, 1, 4><<<grid, 256, 0, st>>>(a, gr); break;
-    case 13: step_f32_group2<MAXBS, 1, 6><<<grid, 256, 0, st>>>(a, gr); break;
-    default: step_f32_group2<MAXBS, 1, 8><<<grid, 256, 0, st>>>(a, gr); break;
-  }
-}
-
 cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const GroupArgs* gr,
                                 int precision, int max_slice_entries, int variant,
                                 cudaStream_t st) {
   const int threads = 256;
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
-    if (variant >= 1 && variant <= 3 && gr) return launch_group64(a, *gr, variant, st);
+    if (variant >= 1 && variant <= 3 && gr) return launch_group64_variant(a, *gr, variant, st);
     step_batched<double, 1><<<a.n_slices, threads, smem, st>>>(a);
   } else if ((a.R == 16 || a.R == 32) && variant >= 16 && variant <= 22 && gr) {
     int maxbs = 1;
@@ -1367,21 +905,19 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
     if (maxbs > 2) {
       step_batched<float, 1><<<a.n_slices, threads, smem, st>>>(a);
     } else if (a.R == 32) {
-      launch_group4<8>(a, *gr, variant, st);
+      launch_group4_variant(8, a, *gr, variant, st);
     } else {
-      launch_group4<4>(a, *gr, variant, st);
+      launch_group4_variant(4, a, *gr, variant, st);
     }
   } else if (a.R % 64 == 0 && variant >= 9 && variant <= 22 && gr) {
     int maxbs = 1;
     for (int k = 0; k < gr->n_groups; ++k) maxbs = gr->bs[k] > maxbs ? gr->bs[k] : maxbs;
     if (variant >= 16 && maxbs <= 2) {
-      if (a.R % 64 == 0) launch_group4<16>(a, *gr, variant, st);
-      else if (a.R == 32) launch_group4<8>(a, *gr, variant, st);
-      else launch_group4<4>(a, *gr, variant, st);
+      launch_group4_variant(a.R % 64 == 0 ? 16 : a.R == 32 ? 8 : 4, a, *gr, variant, st);
     } else if (maxbs <= 2) {
-      launch_group2<2>(a, *gr, variant >= 16 ? 14 : variant, st);
+      launch_group2_variant(2, a, *gr, variant >= 16 ? 14 : variant, st);
     } else {
-      launch_group2<3>(a, *gr, variant >= 16 ? 14 : variant, st);
+      launch_group2_variant(3, a, *gr, variant >= 16 ? 14 : variant, st);
     }
   } else if (a.R % 64 == 0 && variant == 8 && gr) {
     static std::atomic<uint64_t> attr_set{0};

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "bfe_device.cuh"
 #include "bfe_internal.h"
 
 namespace bfe {
@@ -75,39 +76,6 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
 
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-}
-
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
-  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
-}
-
-__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
-  s = __fadd2_rn(a, b);
-  const float2 bb = f2sub(s, a);
-  e = __fadd2_rn(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
-}
-
-__device__ __forceinline__ int lower_bound_i32(const int32_t* a, int n, int key) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(a + mid) < key) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
-__device__ __forceinline__ float forcing_f32(const StepArgs& a, int i, int r) {
-  const float* coef = static_cast<const float*>(a.frc_coef);
-  const float* sig = static_cast<const float*>(a.sig) + (size_t)step_index(a) * a.n_sig;
-  float f = 0.f;
-  for (int e = lower_bound_i32(a.frc_row, a.n_frc, i); e < a.n_frc && __ldg(a.frc_row + e) == i; ++e)
-    if (__ldg(a.frc_rhs + e) == r) f += __ldg(coef + e) * __ldg(sig + __ldg(a.frc_sig + e));
-  return f;
-}
-
-__device__ __forceinline__ void history(const StepArgs& a, int i, int r, double v) {
-  for (int k = lower_bound_i32(a.mon_row, a.n_mon, i); k < a.n_mon && __ldg(a.mon_row + k) == i; ++k)
-    a.hist[(size_t)__ldg(a.mon_slot + k) + (size_t)a.q * ((size_t)step_index(a) + (size_t)a.n_t * r)] = v;
 }
 
 struct TItem {
@@ -227,7 +195,7 @@ __device__ __forceinline__ void compute_titem(const StepArgs& a, const GroupArgs
     const float2 q2 = make_float2(qv[k], qv[k]);
     float2 inc = __ffma2_rn(q2, d, acc[k]);
     if (info[k] & kRowForced)
-      inc = __fadd2_rn(inc, make_float2(forcing_f32(a, row, c), forcing_f32(a, row, c + 1)));
+      inc = __fadd2_rn(inc, make_float2(forcing_sum<float>(a, row, c), forcing_sum<float>(a, row, c + 1)));
     inc = __ffma2_rn(q2, err, inc);
     const float2 r = __fadd2_rn(uo[k], inc);
     *reinterpret_cast<float2*>(unew + o) = r;
@@ -236,8 +204,8 @@ __device__ __forceinline__ void compute_titem(const StepArgs& a, const GroupArgs
       const float2 vi = a.int_base_prev ? __fadd2_rn(__fadd2_rn(d, err), inc) : __fadd2_rn(d, err);
       *reinterpret_cast<float2*>(static_cast<float*>(a.v_int) + (size_t)tt * R + c) = vi;
     } else if (info[k] & kRowMonitored) {
-      history(a, row, c, (double)r.x);
-      history(a, row, c + 1, (double)r.y);
+      write_history(a, row, c, (double)r.x);
+      write_history(a, row, c + 1, (double)r.y);
     }
   }
 }
