@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink the model size (testing only; 1.0 = the benchmark model)")
     ap.add_argument("--n-t", type=int, default=None)
+    ap.add_argument("--sources", type=int, default=None,
+                    help="array elements = right-hand sides (default 64, the benchmark; at most 64)")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the extra sections (C0 plate, FMC, assembly, 3D, adjoint); runs with "
                          "more than one GPU always skip them")
@@ -209,6 +211,10 @@ def run_ours(args):
     from bfe_gb300 import model
     w = workload(args.scale)
     w["scale"] = args.scale
+    if args.sources:
+        if not 1 <= args.sources <= 64:
+            raise SystemExit("--sources must be between 1 and 64")
+        w["n_src"] = args.sources
     n_t = args.n_t or w["n_t"]
     t0 = time.perf_counter()
     main, subs = build_workload(w, args.subdomains)
@@ -427,10 +433,10 @@ def run_ours(args):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batched multi-source and multi-model: coupled water/steel "
                                    "60x30 mm at 0.05 mm (1.44M triangles, ASI2D2 interface, quadratic "
-                                   "absorbers, void blob) with a 64-element array, plus %d steel "
+                                   "absorbers, void blob) with a %d-element array, plus %d steel "
                                    "scatterer sub-domain models of 50k-400k DOF (absorbers, void), "
-                                   "one plan, 64 sources as 64 RHS, %d samples, FP32 batched, CUDA graph"
-                                   % (len(subs), n_t),
+                                   "one plan, %d sources as %d RHS, %d samples, FP32 batched, CUDA graph"
+                                   % (R, len(subs), R, R, n_t),
                        "n_dof": n, "nnz_K": int(nnz), "models": len(models), "sources": R,
                        "monitors": q, "samples": n_t, "steps_marched_per_source": steps_per_march,
                        "l2": "inputs larger than L2 (state %.0f MB per time step)" % (3 * R * n * 4 / 1e6),
