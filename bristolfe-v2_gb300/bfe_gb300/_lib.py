@@ -44,25 +44,31 @@ VP = ctypes.c_void_p
 
 
 class BfeSparse(ctypes.Structure):
+    """bfe_sparse: a CSR or CSC view (0-based int64 indices, FP64 values)."""
     _fields_ = [("n_rows", I64), ("n_cols", I64), ("nnz", I64), ("format", I32),
                 ("ptr", PI64), ("idx", PI64), ("val", PD)]
 
 
 class BfeMesh2d(ctypes.Structure):
+    """bfe_mesh2d: nodes, zero-padded 1-based element lists, materials,
+    absorbing indices and element types (BFE_EL_*)."""
     _fields_ = [("n_nodes", I64), ("nds", PD), ("n_el", I64), ("el_cols", I32), ("els", PI64),
                 ("el_mat", PI32), ("el_abs", PD), ("el_typ", PI32)]
 
 
 class BfeMaterial(ctypes.Structure):
+    """bfe_material: element type, density and the 6 x 6 (or scalar) D."""
     _fields_ = [("el_typ", I32), ("rho", ctypes.c_double), ("D", ctypes.c_double * 36)]
 
 
 class BfeAssemblyOptions(ctypes.Structure):
+    """bfe_assembly_options: DOFs in use (bit mask) and the absorber grading."""
     _fields_ = [("dof_mask", I32), ("damping_power_law", ctypes.c_double),
                 ("max_damping", ctypes.c_double), ("max_stiffness_reduction", ctypes.c_double)]
 
 
 class BfeStats(ctypes.Structure):
+    """bfe_stats: counters of a plan's last run (bfe_plan_stats)."""
     _fields_ = [("step_launches", I64), ("aux_launches", I64), ("step_ms", ctypes.c_double),
                 ("aux_ms", ctypes.c_double), ("n_dof", I64), ("nnz_stored", I64),
                 ("nnz_padded", I64), ("n_interface", I64), ("n_direct_rows", I64),
@@ -143,6 +149,7 @@ def load():
 
 
 def check(status):
+    """Raise BfeError with bfe_last_error()'s message unless status is BFE_OK."""
     if status != BFE_OK:
         msg = load().bfe_last_error()
         raise BfeError(status, msg.decode() if msg else "")

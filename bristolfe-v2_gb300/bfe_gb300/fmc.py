@@ -13,8 +13,10 @@ from .solver import VEL_CURRENT, VEL_LAST_HALF, SolverError, _csr_view
 
 
 def fn_convolve_gb300(f, g, dim=1):
-    """fn_convolve(f, g, dim) for dim = 1 (each column of f with g; a vector
-    f is one signal). Returns an array shaped like f."""
+    """fn_convolve(f, g, dim) (code/internal/fn_convolve.m:22-33) on the GPU
+    for dim = 1: each column of f with g, as the 2 size(f, 1)-point FFT
+    convolution truncated to size(f) (a direct sum here, wrap-around
+    included). A vector f is one signal. Returns an array shaped like f."""
     if dim != 1:
         raise SolverError("only dim = 1 (columns) is supported")
     f = np.asarray(f, float)
@@ -44,7 +46,8 @@ def _pair_lists(tx, rx, mon_nds_of_step, trans_nds, trans_wts):
 
 
 def fn_parse_to_fmc_gb300(tx, rx, mon_nds_of_step, dsps_of_step, trans_nds, trans_wts, in_sig):
-    """fn_parse_to_fmc on the GPU (0-based tx, rx per pair). dsps_of_step is
+    """fn_parse_to_fmc (subdoms/fn_run_main_model.m:239-256) on the GPU
+    (0-based tx, rx per pair). dsps_of_step is
     a list of per-step (q, n_t) displacement arrays, or one (q, n_t, R) array
     (e.g. Plan.run_batched's history); returns time_data (n_t, n_pairs)."""
     if isinstance(dsps_of_step, np.ndarray) and dsps_of_step.ndim == 3:
@@ -85,8 +88,9 @@ def fmc_from_device_history(d_hist, q, n_t, R, tx, rx_slots, rx_weights, in_sig,
 
 
 def fn_convert_disps_to_forces_v2_gb300(K_sub, C_sub, M_sub, time_step, disp_inp, lyrs, in_or_out, solver_mode):
-    """fn_convert_disps_to_forces_v2 on the GPU: returns (force_inp,
-    force_set, force_in_set, force_out_set) like the reference."""
+    """fn_convert_disps_to_forces_v2 (code/fn_convert_disps_to_forces_v2.m:1-31)
+    on the GPU: returns (force_inp, force_set, force_in_set, force_out_set)
+    like the reference."""
     if in_or_out not in ("in", "out"):
         raise SolverError("in_or_out must be 'in' or 'out'")
     modes = {VEL_CURRENT: _lib.BFE_MODE_VEL_CURRENT, VEL_LAST_HALF: _lib.BFE_MODE_VEL_LAST_HALF}

@@ -66,6 +66,8 @@ def rect_mesh(x0, x1, y0, y1, h):
 
 
 def centroids(nds, els):
+    """Element centres: mean of each element's node coordinates (zero-padded
+    node lists, fn_calc_element_centres.m)."""
     m = (els > 0).sum(1, keepdims=True)
     idx = np.where(els > 0, els, 1) - 1
     return (nds[idx] * (els > 0)[:, :, None]).sum(1) / m
@@ -115,6 +117,8 @@ def distance_to_polygon(pts, poly):
 
 
 def remove_unused_nodes(nds, els):
+    """Drop nodes no element uses and renumber the elements' 1-based node
+    lists in the original order."""
     used = np.unique(els[els > 0])
     remap = np.zeros(nds.shape[0] + 1, np.int64)
     remap[used] = np.arange(1, used.size + 1)
@@ -169,6 +173,10 @@ def _select(dofs_all, nodes_all, keep):
 
 
 def cpe3(nds, e, D, rho, keep):
+    """Plane-strain constant-strain triangles (fn_el_CPE3.m:47-155): K = A B'DB
+    with the 6 x 6 D and engineering shear, lumped M = rho J / 6 per DOF,
+    no C; DOFs of `keep` (1-3) per node, node-major. Returns (K, C, M,
+    local node, local DOF) per element."""
     J, gx, gy = _tri_grads(nds, e)
     n = e.shape[0]
     # strain rows [e11, e22, e33, g23, g13, g12]; local dof order (node, dof 1..3)
@@ -190,6 +198,8 @@ def cpe3(nds, e, D, rho, keep):
 
 
 def ac2d3(nds, e, bulk, rho, keep):
+    """Acoustic pressure triangles (fn_el_AC2D3.m:47-77): K = -(grad N . grad N)
+    A / rho, lumped M = -A / (3 bulk), DOF 4 only."""
     J, gx, gy = _tri_grads(nds, e)
     sel, ln, ld = _select(np.array([4, 4, 4]), np.array([1, 2, 3]), keep)
     G = gx[:, :, None] * gx[:, None, :] + gy[:, :, None] * gy[:, None, :]
@@ -201,6 +211,9 @@ def ac2d3(nds, e, bulk, rho, keep):
 
 
 def asi2d2(nds, e, keep):
+    """Fluid-solid interface lines (fn_el_ASI2D2.m:49-79): an 8 x 8 C coupling
+    the solid DOFs 1-2 of both nodes to the fluid DOF 4 with +-L/4 times the
+    unit normal pointing into the fluid; no K or M."""
     p1 = nds[e[:, 0] - 1]
     p2 = nds[e[:, 1] - 1]
     d = p1 - p2
@@ -265,6 +278,7 @@ def assemble(nds, els, el_mat, el_abs, typ, matls, dof_to_use=None, damping_powe
     c = np.concatenate(cols)
 
     def build(vals):
+        # COO triplets summed into CSR (MATLAB sparse), exact zeros dropped
         A = sp.csr_matrix((np.concatenate(vals), (r, c)), shape=(N, N))
         A.sum_duplicates()
         A.eliminate_zeros()
