@@ -55,7 +55,9 @@ def _assemble(ke, mh, ch, dof, n, s, rho_e):
 
 
 def forward(K, m, c, dt, n_t, frc_idx, F, ti0):
-    """All states u_t (n, n_t) of one source, v6 'vel at curent time step'."""
+    """All states u_t (n, n_t) of one source, v6 'vel at curent time step'
+    (code/internal/fn_explicit_dynamic_solver_v6.m:135-138, 185), written
+    with the mass-weighted matrices of this module's header."""
     n = K.shape[0]
     A = m + dt / 2 * c
     E = -m + dt / 2 * c

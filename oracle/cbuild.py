@@ -13,6 +13,8 @@ LIB = os.path.join(OUT_DIR, "libcpu_march.so")
 
 
 def build(force=False):
+    """Compile the C restatement of the v6 loop (OpenMP) into a shared library
+    beside it, unless it is newer than its source; returns the library path."""
     os.makedirs(OUT_DIR, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB

@@ -26,6 +26,7 @@ def _load():
 
 
 def threads():
+    """OpenMP threads the C port uses (all host threads)."""
     return _load().cpu_threads()
 
 
