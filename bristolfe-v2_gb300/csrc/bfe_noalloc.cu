@@ -16,7 +16,6 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
-#include <mutex>
 
 #include "../../include/bfe_gb300.h"
 #include "bfe_internal.h"
@@ -26,13 +25,6 @@ namespace {
 // Largest model the allocation-free march accepts, and its scratch.
 constexpr int64_t kNoAllocMaxDof = int64_t(1) << 20;     // 1,048,576 DOFs
 static __device__ __align__(256) double g_noalloc_state[3 * kNoAllocMaxDof];   // 24 MiB
-
-// Host-side copies of the scratch's device address, one per device, filled
-// by the first call on that device.
-constexpr int kMaxDevices = 64;
-double* g_state_ptr[kMaxDevices] = {nullptr};
-std::mutex g_state_mutex;
-
 
 __global__ void noalloc_step(int32_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                              const double* __restrict__ bv, const double* __restrict__ dv,
@@ -62,19 +54,19 @@ int nfail(int code, const char* msg) {
   return code;
 }
 
-// Device address of the scratch for the current device (set-up on first use).
+// Device address of the scratch for the current device. Looked up on every
+// call: the address belongs to the module loaded in the device's current
+// context, and a context torn down and made again (cudaDeviceReset, a host
+// framework's device reset) loads the module afresh, possibly elsewhere. The
+// lookup is a host-side table read once the module is loaded; the first call
+// on a device also loads the module there.
 int scratch_for_current_device(double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return nfail(BFE_ERR_NO_DEVICE, "no CUDA device available");
-  if (dev < 0 || dev >= kMaxDevices) return nfail(BFE_ERR_UNSUPPORTED, "device index beyond the supported range");
-  std::lock_guard<std::mutex> lock(g_state_mutex);
-  if (!g_state_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_state);
-    if (e != cudaSuccess) return nfail(BFE_ERR_CUDA, cudaGetErrorString(e));
-    g_state_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_state_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_state);
+  if (e != cudaSuccess) return nfail(BFE_ERR_CUDA, cudaGetErrorString(e));
+  *out = static_cast<double*>(p);
   return BFE_OK;
 }
 
@@ -92,6 +84,8 @@ extern "C" int bfe_run_f64_noalloc(int64_t n, const int32_t* d_row_ptr, const in
   if (n > kNoAllocMaxDof)
     return nfail(BFE_ERR_ARG, "model larger than the allocation-free limit of 1048576 DOFs");
   if (n_t < 1 || ti_start < 0 || n_frc < 0 || q < 0) return nfail(BFE_ERR_ARG, "invalid sizes");
+  if (n_frc > INT32_MAX || q > INT32_MAX)
+    return nfail(BFE_ERR_ARG, "n_frc and q must not exceed 2147483647 (int32 kernel indices)");
   if (!d_row_ptr || !d_col || !d_bval || !d_dvec) return nfail(BFE_ERR_ARG, "NULL operator array");
   if (n_frc > 0 && (!d_frc_row || !d_frc_coef || !d_sig)) return nfail(BFE_ERR_ARG, "NULL forcing array");
   if (q > 0 && (!d_hist_row || !d_hist)) return nfail(BFE_ERR_ARG, "NULL history array");

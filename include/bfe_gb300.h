@@ -421,17 +421,24 @@ int bfe_plan_stats(const bfe_plan* plan, bfe_stats* out);
  * keeps until the process exits. Models above 1,048,576 DOFs are rejected
  * with BFE_ERR_ARG.
  *
- * The first call on a device looks the array's address up for that device
- * (make it before any stream capture). Every call clears the state at its
- * start; all calls share the one array, so calls that overlap on the GPU
- * (other streams, other threads) race and must be serialised by the caller.
+ * Every call looks up the array's device address for the current device (a
+ * device reset can move it); the first call on a device also loads the
+ * library's device code there, so make that first call before any stream
+ * capture. Every call clears the state at its start; all calls share the one
+ * array, so calls that overlap on the GPU (other streams, other threads) race
+ * and must be serialised by the caller. n_frc and q are limited to
+ * 2,147,483,647 (BFE_ERR_ARG beyond).
  *
  *   u_{n+1}[i] = sum_j B_ij u_n[j] + d_i u_{n-1}[i]   (+ forcing)
  * B in CSR (d_row_ptr[n+1], d_col, d_bval; 0-based int32) and d the diagonal
  * of D, i.e. the reference's u = A f + B u_-1 + D u_-2 with P diagonal
  * (fn_explicit_dynamic_solver_v6.m:130-139 without fluid-solid coupling in C).
+ * The entry point cannot check that P is diagonal: an operator of a model
+ * with fluid-solid interface elements (off-diagonal C) gives wrong results.
  * Forcing: for each of n_frc entries, u[d_frc_row[e]] += d_frc_coef[e] *
- * d_sig[ti * n_frc + e] (the coefficient is A's diagonal times any weight).
+ * d_sig[ti * n_frc + e] (the coefficient is A's diagonal times any weight);
+ * entries naming the same row add up (the reference's f(idx) = ... keeps
+ * the last one: pass each row once for that behaviour).
  * History: d_hist[k + q * ti] = u[d_hist_row[k]], q x n_t column-major; the
  * caller zeroes it (samples before ti_start are not written).
  */

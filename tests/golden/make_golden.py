@@ -13,8 +13,8 @@ reference's own numbers for those inputs and are stored in
 ``elements_golden.npz`` for the CPU tests, which compare the oracle's
 independently derived element routines against them.
 
-Run in a checkout that has the reference at REFERENCE_ROOT (default
-``/root/reference``); the tests read only the stored fixture.
+Run with the reference checkout's root as the first argument (or in the
+environment variable REFERENCE_ROOT); the tests read only the stored fixture.
 """
 import os
 import re
@@ -22,7 +22,7 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT", "")
 ELDIR = os.path.join(REF, "code", "internal", "elements")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "elements_golden.npz")
 
