@@ -207,8 +207,38 @@ def build_workload(w, n_sub):
     return main, subs
 
 
+def _model_costs(models, R):
+    """Bytes one FP32 time step of each model moves with R sources (the
+    sharding weights)."""
+    return [algorithmic_bytes(m["K"].nnz, m["K"].shape[0], R, 1, len(m["mon_nodes"]), 4) for m in models]
+
+
+def _dof_groups(models, offs):
+    """Row groups of a joined operator for per-group max-normalised errors:
+    each model's fluid (pressure) rows and its solid (displacement) rows."""
+    from bfe_gb300.solver import dof_maps_from_lookup
+    groups = []
+    for k, m in enumerate(models):
+        _, typ = dof_maps_from_lookup(m["gl"], m["K"].shape[0])
+        for fluid in (True, False):
+            rows = np.nonzero((typ == 4) == fluid)[0]
+            if rows.size:
+                groups.append(rows + offs[k])
+    return groups
+
+
+def _max_err(a, b, groups):
+    """Largest per-group max-normalised difference (a against b)."""
+    out = 0.0
+    for g in groups:
+        ref = np.abs(b[g]).max()
+        if ref > 0:
+            out = max(out, float(np.abs(a[g] - b[g]).max() / ref))
+    return out
+
+
 def run_ours(args):
-    from bfe_gb300 import model
+    from bfe_gb300 import model, shard
     w = workload(args.scale)
     w["scale"] = args.scale
     if args.sources:
@@ -228,6 +258,7 @@ def run_ours(args):
     dist = None
     if world > 1:
         import torch.distributed as dist
+        torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     bfe_gb300.load()
@@ -235,27 +266,30 @@ def run_ours(args):
     dt = min(m["dt"] for m in models)
     t = np.arange(n_t) * dt
     sig = model.toneburst(t, w["fc"], w["cycles"])
-    R = w["n_src"]
+    R_all = w["n_src"]
+    # this rank's share: models by cost (all sources), or sources when ranks
+    # outnumber models; one rank marches everything
+    mine, (s_lo, s_hi) = shard.rank_share(_model_costs(models, R_all), R_all, world, rank)
+    R = s_hi - s_lo
+    sel_models = [models[k] for k in mine]
     t0 = time.perf_counter()
-    plan32, offs = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], m["gl"]) for m in models], dt,
+    plan32, offs = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], m["gl"]) for m in sel_models], dt,
                                         bfe_gb300.VEL_CURRENT, "single")
-    plan64, _ = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], None) for m in models], dt,
-                                     bfe_gb300.VEL_CURRENT, "double")
     t_plan = time.perf_counter() - t0
     n = plan32.n
-    nnz = sum(m["K"].nnz for m in models)
-    # sources: RHS r drives element r of the array and source r of every sub-domain
-    srcs = []
-    for r in range(R):
-        parts = [model.global_indices(main["gl"], main["src_nodes"][r], 4)]
-        for k, m in enumerate(subs, start=1):
-            parts.append(model.global_indices(m["gl"], m["src_nodes"][r], 2) + offs[k])
-        srcs.append(np.concatenate(parts))
-    mon_parts = [model.global_indices(main["gl"], main["mon_nodes"], 4)]
-    for k, m in enumerate(subs, start=1):
-        mon_parts.append(model.global_indices(m["gl"], m["mon_nodes"], 2) + offs[k])
+    nnz = sum(m["K"].nnz for m in sel_models)
+
+    def src_dofs(k, m, r):
+        """1-based DOFs of source r in model k: array element r of the coupled
+        model (pressure), source r of a sub-domain model (displacement)."""
+        return model.global_indices(m["gl"], m["src_nodes"][r], 4 if k == 0 else 2)
+
+    srcs = [np.concatenate([src_dofs(k, m, r) + offs[j] for j, (k, m) in enumerate(zip(mine, sel_models))])
+            for r in range(s_lo, s_hi)]
+    mon_parts = [model.global_indices(m["gl"], m["mon_nodes"], 4 if k == 0 else 2) + offs[j]
+                 for j, (k, m) in enumerate(zip(mine, sel_models))]
     mons = np.concatenate(mon_parts)
-    mon_model = np.concatenate([np.full(p.size, k) for k, p in enumerate(mon_parts)])
+    mon_model = np.concatenate([np.full(p.size, j) for j, p in enumerate(mon_parts)])
     q = mons.size
     p_max = max(s_.size for s_ in srcs)
     frc_dof = np.concatenate([s_ - 1 for s_ in srcs])
@@ -277,6 +311,13 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    def reduce(x, op):
+        if dist is None:
+            return x
+        tt = torch.tensor([float(x)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=op)
+        return float(tt.item())
+
     for _ in range(args.warmup):
         march32()
     barrier()
@@ -289,15 +330,18 @@ def run_ours(args):
         ev1.record(stream)
         barrier()
     ms_total = ev0.elapsed_time(ev1)
-    if dist is not None:
-        tt = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_total = float(tt.item())
+    MAX = dist.ReduceOp.MAX if dist is not None else None
+    SUM = dist.ReduceOp.SUM if dist is not None else None
+    ms_total = reduce(ms_total, MAX)                          # the slowest rank
     ms_step = ms_total / args.steps
+    # distinct work of all ranks: each rank's sources x DOFs x steps
+    dof_updates = reduce(float(R * n * steps_per_march), SUM)
+    n_all = sum(m["K"].shape[0] for m in models)
     st32 = plan32.stats()
     launches = args.steps * (st32["step_launches"] + st32["aux_launches"])
-    value = world * R * n * steps_per_march / (ms_step * 1e-3)
+    value = dof_updates / (ms_step * 1e-3)
     h32 = d_hist.cpu().numpy()                                # (R, n_t, q)
+    local_ascans = {k: h32[:, :, mon_model == j] for j, k in enumerate(mine)}
 
     # per-kernel timing pass (CUDA events around every launch, same stream)
     plan32.set_timing(True)
@@ -312,16 +356,113 @@ def run_ours(args):
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_step / (step_avg_ms * 1e-3) / 1e9
 
-    # plain FP64 form on the same models, one source (the middle element)
+    # end to end through the C ABI with host buffers (H2D signals, D2H A-scans)
+    barrier()
+    th0 = time.perf_counter()
+    plan32.run_batched(t, srcs, sig, mons)
+    e2e_s = reduce(time.perf_counter() - th0, MAX)
+    e2e_value = dof_updates / e2e_s
+    h2d = reduce(8 * n_t * R + 8 * (p_max * R + q), SUM)
+    d2h = reduce(8 * q * n_t * R, SUM)
+
+    # A-scans of every model and source on rank 0 (outside the timed region)
+    if dist is not None:
+        ascans = shard.gather_model_ascans(local_ascans, s_lo, R_all, dist)
+    else:
+        ascans = local_ascans
+    if rank == 0:
+        assert sorted(ascans) == list(range(len(models))), "A-scans of some models are missing"
+
+    extra, gates, fp64 = {}, {}, None
+    if world == 1:
+        fp64, gates = fp64_and_oracle_sections(torch, bfe_gb300, model, models, plan32, offs, srcs, mons,
+                                               mon_model, h32, d_sig, stream, t, sig, dt, ti0, nnz, value,
+                                               args.no_extra)
+        # the extra sections run in one-GPU runs only: under torchrun the
+        # other ranks would hold their GPUs idle in the final barrier meanwhile
+        if not args.no_extra:
+            extra.update(subsection_rooflines(torch, bfe_gb300, models, offs, frc_dof, frc_rhs, frc_sig,
+                                              mons, march32, R, n_t, ti0, peak, dt, stream))
+            extra["plate_c0"] = plate_c0_section(bfe_gb300, model)
+            extra["coupled_c1"] = coupled_c1_section(torch, bfe_gb300, model, main, peak)
+            extra["fmc_c2a"] = fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, mon_parts[0].size, sig, stream)
+            extra["assembly_c1"] = assembly_section(torch, bfe_gb300, model, main)
+            extra["hex3d_c3"] = hex3d_section(torch, bfe_gb300, model)
+            extra["adjoint_c4"] = adjoint_section(torch, bfe_gb300, model)
+    result = None
+    if rank == 0:
+        cpu = gates.pop("_cpu_baseline", None)
+        n_sub = len(subs)
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched multi-source and multi-model: coupled water/steel "
+                                   "60x30 mm at 0.05 mm (1.44M triangles, ASI2D2 interface, quadratic "
+                                   "absorbers, void blob) with a %d-element array, plus %d steel "
+                                   "scatterer sub-domain models of 50k-400k DOF (absorbers, void), "
+                                   "%d sources as %d RHS, %d samples, FP32 batched, CUDA graph"
+                                   % (R_all, n_sub, R_all, R_all, n_t),
+                       "n_dof": n_all, "nnz_K": int(sum(m["K"].nnz for m in models)), "models": len(models),
+                       "sources": R_all, "monitors": int(sum(len(m["mon_nodes"]) for m in models)),
+                       "samples": n_t, "steps_marched_per_source": steps_per_march,
+                       "l2": "inputs larger than L2 (state %.0f MB per time step on rank 0)" % (3 * R * n * 4 / 1e6),
+                       "parallelism": ("one GPU" if world == 1 else
+                                       "%d ranks, models split by cost, no data-path collective" % world),
+                       "rank0_share": {"models": len(mine), "n_dof": n, "sources": [s_lo, s_hi]},
+                       "scale": args.scale},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": profiled_traffic(kname, n),
+                         "kernel": kname, "variant": stk["variant"], "bytes_per_launch": bytes_step,
+                         "avg_launch_ms": step_avg_ms, "peak_source": peak_kind,
+                         "interface_kernel_avg_ms": aux_avg_ms},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+            "setup_s": {"model_build": t_build, "plans": t_plan},
+            "cpu_baseline": cpu,
+        }
+        result.update(extra)
+        # the headline gates last, so that a tail of the line keeps them
+        if fp64 is not None:
+            result["fp64_plain"] = fp64
+        result["gates"] = gates
+        print(json.dumps(result), flush=True)
+    plan32.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return result
+
+
+def fp64_and_oracle_sections(torch, bfe_gb300, model, models, plan32, offs, srcs, mons, mon_model, h32,
+                             d_sig, stream, t, sig, dt, ti0, nnz, value, quick=False):
+    """One-GPU checks of the headline result (the middle source r):
+      - the plain FP64 GPU form on the same models (its DOF-updates/s and the
+        FP32 batched speed-up over it, the metric's comparison);
+      - the FP32 batched A-scans against that FP64 run over all samples;
+      - the FP64 C port of the reference's v6 loop on the joined operator
+        (the CPU baseline, timed on a bounded prefix of the march) as the
+        oracle: the FP32 batched and the FP64 A-scans, and FP32 field frames
+        of the same source (one-source run on the FP32 plan), against it.
+    Errors are max-normalised per model and per kind of DOF (pressure,
+    displacement). Returns (fp64 dict, gates dict with the CPU baseline
+    under "_cpu_baseline")."""
+    R, n_t, q = h32.shape
+    n = plan32.n
     r_mid = R // 2
-    sel = frc_rhs == r_mid
+    plan64, _ = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], None) for m in models], dt,
+                                     bfe_gb300.VEL_CURRENT, "double")
     d_hist64 = torch.zeros((1, n_t, q), dtype=torch.float64, device="cuda")
+    src = srcs[r_mid]
 
     def march64():
         with torch.cuda.stream(stream):
             d_hist64.zero_()
-        plan64.run_device(1, n_t, ti0, frc_dof[sel], np.zeros(sel.sum(), np.int64),
-                          frc_sig[sel], None, d_sig, mons - 1, d_hist64, stream.cuda_stream)
+        plan64.run_device(1, n_t, ti0, src - 1, np.zeros(src.size, np.int64), np.zeros(src.size, np.int64),
+                          None, d_sig, mons - 1, d_hist64, stream.cuda_stream)
     march64()
     torch.cuda.synchronize()
     k64 = 2
@@ -332,7 +473,7 @@ def run_ours(args):
     e1.record(stream)
     torch.cuda.synchronize()
     ms64 = e0.elapsed_time(e1) / k64
-    value64 = n * steps_per_march / (ms64 * 1e-3)
+    value64 = n * (n_t - ti0) / (ms64 * 1e-3)
     plan64.set_timing(True)
     march64()
     torch.cuda.synchronize()
@@ -340,28 +481,47 @@ def run_ours(args):
     plan64.set_timing(False)
     step64_ms = st64["step_ms"] / max(st64["step_launches"], 1)
     aux64_ms = st64["aux_ms"] / max(st64["aux_launches"], 1)
-    bytes64 = algorithmic_bytes(nnz, n, 1, srcs[r_mid].size, q, 8)
-    h64 = d_hist64.cpu().numpy()[0]
-    # max-normalised A-scan error per model (pressure and displacement differ in units)
-    errs = []
-    for k in range(len(models)):
-        c = mon_model == k
-        errs.append(float(np.abs(h32[r_mid][:, c] - h64[:, c]).max() / max(np.abs(h64[:, c]).max(), 1e-300)))
-    err = max(errs)
+    bytes64 = algorithmic_bytes(nnz, n, 1, src.size, q, 8)
+    h64 = d_hist64.cpu().numpy()[0]                       # (n_t, q)
+    plan64.close()
+    mon_groups = [np.nonzero(mon_model == k)[0] for k in range(len(models))]
+    err_fp64 = _max_err(h32[r_mid].T, h64.T, mon_groups)
+    fp64 = {"value": value64, "unit": UNIT, "ms_per_march": ms64, "step_kernel_ms": step64_ms,
+            "interface_kernel_ms": aux64_ms, "step_kernel_gbs": bytes64 / (step64_ms * 1e-3) / 1e9}
 
-    # the coupled FMC model alone (its own plan), same march
-    plan_a = bfe_gb300.Plan(main["K"], main["C"], main["M"], dt, bfe_gb300.VEL_CURRENT, "single", main["gl"])
-    selm = frc_dof < offs[1]
-    mons_a = mon_parts[0]
-    hist_a = torch.zeros((R, n_t, mons_a.size), dtype=torch.float64, device="cuda")
-    march32(plan_a, hist_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, R)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    march32(plan_a, hist_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, R)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_a = e0.elapsed_time(e1)
-    value_a = R * main["K"].shape[0] * steps_per_march / (ms_a * 1e-3)
+    # the oracle: FP64 C port on the joined operator, a bounded prefix
+    import scipy.sparse as sp
+    Kj = sp.block_diag([m["K"] for m in models], format="csr")
+    Cj = sp.block_diag([m["C"] for m in models], format="csr")
+    Mj = sp.block_diag([m["M"] for m in models], format="csr")
+    cpu, (ho, fo, fto, steps, every) = cpu_baseline(Kj, Cj, Mj, dt, t, src, sig, mons,
+                                                    target_s=4.0 if quick else 10.0)
+    cpu["sample"] += ", all %d models joined in one operator" % len(models)
+    err32_orc = _max_err(h32[r_mid][:steps].T, ho, mon_groups)
+    err64_orc = _max_err(h64[:steps].T, ho, mon_groups)
+    # FP32 frames of the same source from a one-source run on the FP32 plan
+    _, f32, ft32 = plan32.run(t[:steps], src, sig[:steps], mons, every, True)
+    groups = _dof_groups(models, offs)
+    frame_err = _max_err(f32, fo, groups)
+    gates = {"speedup_fp32_batched_vs_fp64_plain": value / value64,
+             "ascan_err_vs_fp64": err_fp64,
+             "ascan_err_vs_oracle": err32_orc, "ascan_err_fp64_vs_oracle": err64_orc,
+             "frame_err_vs_oracle": frame_err,
+             "oracle_check": "source %d of %d, first %d of %d samples, %d frames, FP64 C port of the v6 loop; "
+                             "max-normalised per model and DOF kind" % (r_mid, R, steps, n_t, fo.shape[1]),
+             "frame_times_match": bool(np.array_equal(ft32, fto)),
+             "_cpu_baseline": cpu}
+    return fp64, gates
+
+
+def subsection_rooflines(torch, bfe_gb300, models, offs, frc_dof, frc_rhs, frc_sig, mons, march32, R, n_t,
+                         ti0, peak, dt, stream):
+    """The coupled FMC model alone (its own plan) and the 32 sub-domain
+    models alone (one multi-model plan), same march: DOF-updates/s and the
+    step kernel's roofline."""
+    main, subs = models[0], models[1:]
+    steps_per_march = n_t - ti0
+    out = {}
 
     def part_roofline(plan, dofs, rhs, fsig, mon, n_part, nnz_part, p_part):
         plan.set_timing(True)
@@ -376,99 +536,33 @@ def run_ours(args):
                 "frac_of_measured_hbm": by / ms_ / 1e6 / peak,
                 "kernel": KERNEL_NAMES.get(st_["variant"], "variant %d" % st_["variant"])}
 
+    plan_a = bfe_gb300.Plan(main["K"], main["C"], main["M"], dt, bfe_gb300.VEL_CURRENT, "single", main["gl"])
+    selm = frc_dof < offs[1]
+    mons_a = mons[mons <= offs[1]]
+    hist_a = torch.zeros((R, n_t, mons_a.size), dtype=torch.float64, device="cuda")
+    march32(plan_a, hist_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, R)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    march32(plan_a, hist_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, R)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_a = e0.elapsed_time(e1)
     part_a = part_roofline(plan_a, frc_dof[selm], frc_rhs[selm], frc_sig[selm], mons_a, main["K"].shape[0],
                            main["K"].nnz, max(int((frc_rhs[selm] == r).sum()) for r in range(R)))
     plan_a.close()
-    # the 32 sub-domain models alone (C2b), one multi-model plan
-    part_b = None
+    out["coupled_fmc_only"] = {"value": R * main["K"].shape[0] * steps_per_march / (ms_a * 1e-3), "unit": UNIT,
+                               "ms_per_march": ms_a, "n_dof": int(main["K"].shape[0]), "roofline": part_a}
     if subs:
-        plan_b, offs_b = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], m["gl"]) for m in subs], dt,
-                                              bfe_gb300.VEL_CURRENT, "single")
+        plan_b, _ = bfe_gb300.Plan.multi([(m["K"], m["C"], m["M"], m["gl"]) for m in subs], dt,
+                                         bfe_gb300.VEL_CURRENT, "single")
         sel_b = frc_dof >= offs[1]
         mons_b = mons[mons > offs[1]] - offs[1]
-        part_b = part_roofline(plan_b, frc_dof[sel_b] - offs[1], frc_rhs[sel_b], frc_sig[sel_b], mons_b,
-                               plan_b.n, sum(m["K"].nnz for m in subs),
-                               max(int((frc_rhs[sel_b] == r).sum()) for r in range(R)))
+        out["subdomains_only"] = part_roofline(plan_b, frc_dof[sel_b] - offs[1], frc_rhs[sel_b], frc_sig[sel_b],
+                                               mons_b, plan_b.n, sum(m["K"].nnz for m in subs),
+                                               max(int((frc_rhs[sel_b] == r).sum()) for r in range(R)))
         plan_b.close()
-
-    # end to end through the C ABI with host buffers (H2D signals, D2H A-scans)
-    e2e_steps = 1
-    barrier()
-    th0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        plan32.run_batched(t, srcs, sig, mons)
-    e2e_s = (time.perf_counter() - th0) / e2e_steps
-    if dist is not None:                      # the slowest rank, as for the device-timed value
-        te = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e_s = float(te.item())
-    e2e_value = world * R * n * steps_per_march / e2e_s
-    h2d = 8 * n_t * R + 8 * (p_max * R + q)
-    d2h = 8 * q * n_t * R
-
-    extra = {}
-    # the extra sections run in one-GPU runs only: under torchrun the other
-    # ranks would hold their GPUs idle in the final barrier meanwhile
-    if rank == 0 and world == 1 and not args.no_extra:
-        extra["plate_c0"] = plate_c0_section(bfe_gb300, model)
-        extra["coupled_c1"] = coupled_c1_section(torch, bfe_gb300, model, main, peak)
-        extra["fmc_c2a"] = fmc_section(torch, bfe_gb300, d_hist, R, n_t, q, mon_parts[0].size, sig, stream)
-        extra["assembly_c1"] = assembly_section(torch, bfe_gb300, model, main)
-        extra["hex3d_c3"] = hex3d_section(torch, bfe_gb300, model)
-        extra["adjoint_c4"] = adjoint_section(torch, bfe_gb300, model)
-    result = None
-    if rank == 0:
-        cpu = None
-        if world == 1:
-            import scipy.sparse as sp
-            Kj = sp.block_diag([m["K"] for m in models], format="csr")
-            Cj = sp.block_diag([m["C"] for m in models], format="csr")
-            Mj = sp.block_diag([m["M"] for m in models], format="csr")
-            cpu = cpu_baseline(Kj, Cj, Mj, dt, t, srcs[r_mid], sig, mons)
-            cpu["sample"] += ", all %d models joined in one operator" % len(models)
-        result = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched multi-source and multi-model: coupled water/steel "
-                                   "60x30 mm at 0.05 mm (1.44M triangles, ASI2D2 interface, quadratic "
-                                   "absorbers, void blob) with a %d-element array, plus %d steel "
-                                   "scatterer sub-domain models of 50k-400k DOF (absorbers, void), "
-                                   "one plan, %d sources as %d RHS, %d samples, FP32 batched, CUDA graph"
-                                   % (R, len(subs), R, R, n_t),
-                       "n_dof": n, "nnz_K": int(nnz), "models": len(models), "sources": R,
-                       "monitors": q, "samples": n_t, "steps_marched_per_source": steps_per_march,
-                       "l2": "inputs larger than L2 (state %.0f MB per time step)" % (3 * R * n * 4 / 1e6),
-                       "parallelism": "replicas x%d" % world, "scale": args.scale},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": profiled_traffic(kname, n),
-                         "kernel": kname, "variant": stk["variant"], "bytes_per_launch": bytes_step,
-                         "avg_launch_ms": step_avg_ms, "peak_source": peak_kind,
-                         "interface_kernel_avg_ms": aux_avg_ms},
-            "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_march": ms64,
-                           "step_kernel_ms": step64_ms, "interface_kernel_ms": aux64_ms,
-                           "step_kernel_gbs": bytes64 / (step64_ms * 1e-3) / 1e9,
-                           "speedup_fp32_batched": value / world / value64},
-            "ascan_err_vs_fp64": err,
-            "coupled_fmc_only": {"value": value_a, "unit": UNIT, "ms_per_march": ms_a,
-                                 "n_dof": int(main["K"].shape[0]), "roofline": part_a},
-            "subdomains_only": part_b,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
-            "gpu_launches": launches,
-            "clocks": clocks.summary(),
-            "setup_s": {"model_build": t_build, "plans": t_plan},
-            "cpu_baseline": cpu,
-        }
-        result.update(extra)
-        print(json.dumps(result), flush=True)
-    plan32.close()
-    plan64.close()
-    if dist is not None:
-        dist.barrier()
-        dist.destroy_process_group()
-    return result
+    return out
 
 
 def plate_c0_section(bfe_gb300, model):
@@ -718,18 +812,26 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20, n_t=4000):
     return res
 
 
-def cpu_baseline(K, C, M, dt, t, src_gi, sig, mons, target_s=10.0):
+def cpu_baseline(K, C, M, dt, t, src_gi, sig, mons, target_s=10.0, n_frames=4):
     """The FP64 CPU restatement of the reference's time loop (oracle port) on
-    all host threads, timed on a bounded prefix of one source's march."""
+    all host threads, timed on a bounded prefix of one source's march. The
+    timed march also writes n_frames field frames (velocity); returns the
+    baseline dict and (history q x steps, frames, frame times, steps,
+    frame interval) for the oracle checks."""
     from oracle import cpu_port
     op = cpu_port.CpuOperator(K, C, M, dt)
     n = K.shape[0]
     probe = 20
     _, s = cpu_port.time_march(op, t[:probe], src_gi - 1, sig[None, :probe], mons - 1)
     steps = int(min(len(t), max(probe, target_s / max(s / probe, 1e-9))))
-    _, s = cpu_port.time_march(op, t[:steps], src_gi - 1, sig[None, :steps], mons - 1)
-    return {"value": n * steps / s, "unit": UNIT, "cores": cpu_port.threads(), "kind": "port",
-            "sample": "one source, first %d of %d samples, FP64 v6 loop (C, OpenMP)" % (steps, len(t))}
+    every = max(1, -(-steps // n_frames))
+    t0 = time.perf_counter()
+    hist, fld, fld_t = op.march(t[:steps], src_gi - 1, sig[None, :steps], mons - 1, every, True, frames=True)
+    s = time.perf_counter() - t0
+    return ({"value": n * steps / s, "unit": UNIT, "cores": cpu_port.threads(), "kind": "port",
+             "sample": "one source, first %d of %d samples, %d velocity frames, FP64 v6 loop (C, OpenMP)"
+                       % (steps, len(t), fld.shape[1])},
+            (hist, fld, fld_t, steps, every))
 
 
 def _ref_subdomain(args):
@@ -766,6 +868,11 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", 0))
     if rank != 0:
         return None
+    import shutil
+    # the reference itself is MATLAB code: record whether a MATLAB or GNU
+    # Octave runtime exists on this machine (the timed path is the oracle's C
+    # port of its v6 loop when neither does)
+    runtime_probe = {k: shutil.which(k) for k in ("matlab", "octave", "octave-cli")}
     from oracle import assembly, cpu_port, mesh, signals
     w = workload(args.scale)
     n_t = args.n_t or w["n_t"]
@@ -840,6 +947,7 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_port.threads(), "kind": "port",
                          "sample": "first %d of %d samples of one source" % (steps, n_t)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_runtime_probe": runtime_probe,
     }
     print(json.dumps(line), flush=True)
     return line

@@ -16,8 +16,11 @@ BFE_ERR_CUDA = 3
 BFE_ERR_NUMERIC = 4
 BFE_ERR_UNSUPPORTED = 5
 BFE_ERR_NO_DEVICE = 6
+BFE_ERR_UNSTABLE = 7
+BFE_ERR_TIMEOUT = 8
 STATUS_NAMES = {0: "BFE_OK", 1: "BFE_ERR_ARG", 2: "BFE_ERR_OOM", 3: "BFE_ERR_CUDA",
-                4: "BFE_ERR_NUMERIC", 5: "BFE_ERR_UNSUPPORTED", 6: "BFE_ERR_NO_DEVICE"}
+                4: "BFE_ERR_NUMERIC", 5: "BFE_ERR_UNSUPPORTED", 6: "BFE_ERR_NO_DEVICE",
+                7: "BFE_ERR_UNSTABLE", 8: "BFE_ERR_TIMEOUT"}
 
 BFE_CSR = 0
 BFE_CSC = 1
@@ -116,6 +119,7 @@ SIGNATURES = {
                                    I64, PI64, PD, I64, PD, PD, PD, PD]),
     "bfe_run_f64_noalloc": (I32, [I64, VP, VP, VP, VP, I64, I64, I64, VP, VP, VP, I64, VP, VP, VP]),
     "bfe_plan_set_timing": (I32, [VP, I32]),
+    "bfe_plan_set_time_limit": (I32, [VP, ctypes.c_double]),
     "bfe_plan_stats": (I32, [VP, ctypes.POINTER(BfeStats)]),
     "bfe_last_error": (ctypes.c_char_p, []),
     "bfe_version": (I32, [PI32, PI32, PI32]),
@@ -125,10 +129,14 @@ _lib = None
 
 
 class BfeError(RuntimeError):
-    """A non-zero status returned across the C ABI."""
+    """A non-zero status returned across the C ABI.
 
-    def __init__(self, status, message):
+    For BFE_ERR_UNSTABLE and BFE_ERR_TIMEOUT the run's outputs were still
+    written; ``outputs`` then holds what the call would have returned."""
+
+    def __init__(self, status, message, outputs=None):
         self.status = status
+        self.outputs = outputs
         super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
 
 
@@ -148,11 +156,13 @@ def load():
     return lib
 
 
-def check(status):
-    """Raise BfeError with bfe_last_error()'s message unless status is BFE_OK."""
+def check(status, outputs=None):
+    """Raise BfeError with bfe_last_error()'s message unless status is BFE_OK
+    (``outputs`` is attached for the statuses after which they are valid)."""
     if status != BFE_OK:
         msg = load().bfe_last_error()
-        raise BfeError(status, msg.decode() if msg else "")
+        keep = outputs if status in (BFE_ERR_UNSTABLE, BFE_ERR_TIMEOUT) else None
+        raise BfeError(status, msg.decode() if msg else "", keep)
 
 
 def ptr(a, ctype):

@@ -167,6 +167,12 @@ class Plan:
         """CUDA-event timing of every launch in later runs (see stats())."""
         check(self._lib.bfe_plan_set_timing(self._h, int(bool(enable))))
 
+    def set_time_limit(self, seconds):
+        """Wall-clock limit of later runs (0 = none): a run that passes it
+        stops and raises BfeError(BFE_ERR_TIMEOUT) carrying the outputs
+        computed so far."""
+        check(self._lib.bfe_plan_set_time_limit(self._h, float(seconds)))
+
     def stats(self):
         """Counters of the last run as a dict (launches, device ms, nnz, ...)."""
         st = _lib.BfeStats()
@@ -227,7 +233,7 @@ class Plan:
             st = self._lib.bfe_run_field(self._h, field.handle, *args)
         else:
             st = self._lib.bfe_run(self._h, *args)
-        check(st)
+        check(st, (hist, fld, fld_t))
         return hist, fld, fld_t
 
     def run_v5(self, time, forcing_indices, forcing_functions, disp_indices, disp_functions,
@@ -281,7 +287,7 @@ class Plan:
                                   ptr(D, ctypes.c_double), q, ptr(hi, ctypes.c_int64), every,
                                   ptr(hist, ctypes.c_double), ptr(fld, ctypes.c_double),
                                   ptr(fld_t, ctypes.c_double), ptr(frc, ctypes.c_double))
-        check(st)
+        check(st, (hist, fld, frc, fld_t))
         return hist, fld, frc, fld_t
 
     def run_batched(self, time, forcing_indices_per_source, forcing_functions, history_indices):
@@ -312,7 +318,7 @@ class Plan:
         st = self._lib.bfe_run_batched(self._h, R, nt, ptr(time, ctypes.c_double), p,
                                        ptr(fi, ctypes.c_int64), rows, ptr(F, ctypes.c_double),
                                        q, ptr(hi, ctypes.c_int64), ptr(hist, ctypes.c_double))
-        check(st)
+        check(st, hist)
         return hist
 
     def adjoint_gradient(self, element_data, time, forcing_indices_per_source, forcing_functions,

@@ -4,6 +4,7 @@
 // bfe_run_field / bfe_run_v5) and bfe_adjoint_host.cpp (bfe_adjoint_gradient).
 #pragma once
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -153,6 +154,8 @@ struct bfe_plan {
   int64_t nnz_padded = 0;
   int64_t n_direct_rows = 0;
   bool timing = false;
+  double time_limit_s = 0.0;        // wall-clock limit of a run (0 = none)
+  bfe_host::DevBuf<int> d_flag;     // non-finite flag of the last run
   bfe_stats last{};
   // autotuned batched-kernel variant per R (chosen on the first run with that R)
   std::map<int64_t, int> variant_of_R;
@@ -235,6 +238,7 @@ int prepare_run(bfe_plan* pl, std::vector<ForceEntry>& frc, const std::vector<in
                 int64_t R, int64_t n_t, int64_t n_sig, const double* d_sig64, double* d_hist,
                 cudaStream_t st, RunArrays& ra, bfe::StepArgs& a);
 int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st);
+bool outputs_valid(int rc);
 int64_t first_nonzero_column(const double* frcs, int64_t rows, int64_t n_t, int64_t R);
 int check_time(bfe_plan* pl, int64_t n_t, const double* time);
 int build_forcing(bfe_plan* pl, int64_t R, int64_t p, const int64_t* frc_idx, int64_t frc_rows,

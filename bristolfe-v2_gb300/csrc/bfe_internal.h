@@ -155,6 +155,9 @@ cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const Grou
 size_t batched_smem_bytes(int precision, int max_slice_entries);
 cudaError_t set_batched_smem_limit(int precision, size_t smem);
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);
+// Sets *flag to 1 if any of the count values at u (FP64 for precision 0,
+// FP32 otherwise) is NaN or infinite; leaves it alone otherwise.
+cudaError_t launch_nonfinite_check(const void* u, int64_t count, int precision, int* flag, cudaStream_t s);
 // Group block-sparse kernel families (bfe_group_kernels.cu), by batched
 // variant: packed warp-per-node for block size maxbs (2 or 3), half-warp
 // float4 with lpn lanes per node (16, 8 or 4), FP64 direct form.

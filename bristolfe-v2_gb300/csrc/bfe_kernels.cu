@@ -20,6 +20,7 @@
 //    in a second small kernel: v = (u_hat - u_{n-1}) or (u_n - u_{n-1})
 //    is staged per interface row, then u_new = base + Z v.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 
 #include "bfe_device.cuh"
@@ -979,6 +980,24 @@ cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_
   const int blocks = (int)((total + threads - 1) / threads);
   if (precision == 0) interface_fixup<double><<<blocks, threads, 0, st>>>(a);
   else interface_fixup<float><<<blocks, threads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void nonfinite_kernel(const T* __restrict__ u, int64_t count, int* flag) {
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(u[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) *flag = 1;
+}
+
+cudaError_t launch_nonfinite_check(const void* u, int64_t count, int precision, int* flag, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  const int threads = 256;
+  const int64_t need = (count + threads - 1) / threads;
+  const int blocks = (int)std::min<int64_t>(need, (int64_t)sm_count() * 8);
+  if (precision == 0) nonfinite_kernel<double><<<blocks, threads, 0, st>>>(static_cast<const double*>(u), count, flag);
+  else nonfinite_kernel<float><<<blocks, threads, 0, st>>>(static_cast<const float*>(u), count, flag);
   return cudaGetLastError();
 }
 

@@ -303,7 +303,7 @@ const char* bfe_last_error(void) { return g_last_error.c_str(); }
 
 int bfe_version(int32_t* major, int32_t* minor, int32_t* patch) {
   if (major) *major = 0;
-  if (minor) *minor = 1;
+  if (minor) *minor = 2;
   if (patch) *patch = 0;
   return BFE_OK;
 }
@@ -311,6 +311,13 @@ int bfe_version(int32_t* major, int32_t* minor, int32_t* patch) {
 int bfe_plan_set_timing(bfe_plan* plan, int32_t enable) {
   if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
   plan->timing = enable != 0;
+  return BFE_OK;
+}
+
+int bfe_plan_set_time_limit(bfe_plan* plan, double seconds) {
+  if (!plan) return fail(BFE_ERR_ARG, "plan is NULL");
+  if (!(seconds >= 0.0) || std::isinf(seconds)) return fail(BFE_ERR_ARG, "the time limit must be finite and >= 0");
+  plan->time_limit_s = seconds;
   return BFE_OK;
 }
 

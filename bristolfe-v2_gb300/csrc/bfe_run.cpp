@@ -43,6 +43,41 @@ bool make_state_map(CUtensorMap* m, void* base, int64_t n, int64_t R) {
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Wall-clock limit of one run (bfe_plan_set_time_limit). After each chunk of
+// steps has been queued, wait for the chunk before it (so one chunk stays
+// queued ahead on the GPU) and compare the time since the run began with the
+// limit; once it has passed, the run queues nothing more.
+struct TimeLimit {
+  double limit = 0.0;
+  std::chrono::steady_clock::time_point t0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  int64_t chunks = 0;
+  bool expired = false;
+  ~TimeLimit() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  cudaError_t start(double seconds) {
+    limit = seconds;
+    t0 = std::chrono::steady_clock::now();
+    if (limit <= 0.0) return cudaSuccess;
+    for (cudaEvent_t& e : ev) {
+      const cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+      if (r != cudaSuccess) return r;
+    }
+    return cudaSuccess;
+  }
+  cudaError_t chunk_queued(cudaStream_t st) {
+    if (limit <= 0.0) return cudaSuccess;
+    cudaError_t r = cudaEventRecord(ev[chunks & 1], st);
+    if (r == cudaSuccess && chunks >= 1) r = cudaEventSynchronize(ev[(chunks - 1) & 1]);
+    ++chunks;
+    const std::chrono::duration<double> el = std::chrono::steady_clock::now() - t0;
+    if (el.count() > limit) expired = true;
+    return r;
+  }
+};
+
 }  // namespace
 
 namespace bfe_host {
@@ -173,6 +208,8 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     ~EvGuard() { for (auto e : *a) cudaEventDestroy(e); for (auto e : *b) cudaEventDestroy(e); }
   } guard{&ev_step, &ev_aux};
   const bool timing = pl->timing;
+  TimeLimit limit;
+  CUDA_TRY(limit.start(pl->time_limit_s));
   // Autotuner: on the first batched run with this R, time every kernel
   // variant on a few steps of the real operator (state still zero, so the
   // results are discarded by the real march that follows) and keep the
@@ -349,18 +386,33 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     stt.step_launches = launches0;
     stt.aux_launches = aux0;
     const int64_t reps = (rs.n_t - rs.ti_start) / kGraphSteps;
-    for (int64_t r = 0; r < reps; ++r) CUDA_TRY(cudaGraphLaunch(gexec, st));
-    stt.step_launches += reps * per_step;
-    stt.aux_launches += reps * (per_aux + 1);
-    ti = rs.ti_start + reps * kGraphSteps;      // rotation is back where it started
+    int64_t done = 0;
+    while (done < reps && !limit.expired) {
+      CUDA_TRY(cudaGraphLaunch(gexec, st));
+      ++done;
+      CUDA_TRY(limit.chunk_queued(st));
+    }
+    stt.step_launches += done * per_step;
+    stt.aux_launches += done * (per_aux + 1);
+    ti = rs.ti_start + done * kGraphSteps;      // rotation is back where it started
     a.ti_dev = nullptr;
   }
-  for (; ti < rs.n_t; ++ti) {
+  for (int64_t k = 1; ti < rs.n_t && !limit.expired; ++ti, ++k) {
     a.ti = ti;
     const int rc3 = one_step(ti, true);
     if (rc3) return rc3;
+    if (k % kGraphSteps == 0) CUDA_TRY(limit.chunk_queued(st));
   }
+  // non-finite values anywhere in the march stay in the state (every row's
+  // update includes its own previous value), so one check of the newest
+  // state finds them
+  if (!pl->d_flag.p) CUDA_TRY(pl->d_flag.alloc(1));
+  CUDA_TRY(cudaMemsetAsync(pl->d_flag.p, 0, sizeof(int), st));
+  CUDA_TRY(bfe::launch_nonfinite_check(U[icur], n * R, prec, pl->d_flag.p, st));
+  stt.aux_launches++;
   CUDA_TRY(cudaStreamSynchronize(st));
+  int nonfinite = 0;
+  CUDA_TRY(cudaMemcpy(&nonfinite, pl->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (have_tmaps) {
     int err = 0;
     CUDA_TRY(cudaMemcpy(&err, pl->d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -377,8 +429,17 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     stt.aux_ms += ms;
   }
   CUDA_TRY(cudaStreamSynchronize(st));
+  if (nonfinite)
+    return fail(BFE_ERR_UNSTABLE, "the march produced non-finite values by sample %lld of %lld (time step above "
+                "the stability limit, or non-finite forcing)", (long long)ti, (long long)rs.n_t);
+  if (limit.expired)
+    return fail(BFE_ERR_TIMEOUT, "the run exceeded its time limit of %g s: stopped after sample %lld of %lld",
+                limit.limit, (long long)ti, (long long)rs.n_t);
   return BFE_OK;
 }
+
+// Statuses after which a run's outputs are still copied to the caller.
+bool outputs_valid(int rc) { return rc == BFE_OK || rc == BFE_ERR_UNSTABLE || rc == BFE_ERR_TIMEOUT; }
 
 // First 0-based column with any non-zero |forcing| (v6.m:163-169); n_t if none.
 int64_t first_nonzero_column(const double* frcs, int64_t rows, int64_t n_t, int64_t R) {
@@ -472,13 +533,14 @@ int run_one(bfe_plan* plan, const bfe_field* field, int64_t n_t, const double* t
     rs.d_fld = d_fld.p;
   }
   rs.fld_time = &ftime;
-  if ((rc = execute(plan, rs, st))) return rc;
+  const int xrc = execute(plan, rs, st);
+  if (!outputs_valid(xrc)) return xrc;
   if (hist_n) CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (rows) CUDA_TRY(cudaMemcpyAsync(fld_out, d_fld.p, (size_t)rows * n_frames * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
   if (dev != plan->device) cudaSetDevice(dev);
-  return BFE_OK;
+  return xrc;
 }
 
 }  // namespace bfe_host
@@ -525,13 +587,14 @@ int bfe_run_batched(bfe_plan* plan, int64_t R, int64_t n_t, const double* time,
   CUDA_TRY(d_hist.alloc(hist_n));
   if (hist_n) CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
   rs.d_hist = d_hist.p;
-  if ((rc = execute(plan, rs, st))) return rc;
+  const int xrc = execute(plan, rs, st);
+  if (!outputs_valid(xrc)) return xrc;
   if (hist_n) {
     CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
   }
   if (dev != plan->device) cudaSetDevice(dev);
-  return BFE_OK;
+  return xrc;
 } catch (...) {
   return bfe::exception_status();
 }
@@ -780,7 +843,8 @@ int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,
     rs.d_ud[0] = d_ud.p;
     rs.d_ud[1] = d_ud.p + ns;
   }
-  if ((rc = execute(plan, rs, st))) return rc;
+  const int xrc = execute(plan, rs, st);
+  if (!outputs_valid(xrc)) return xrc;
   if (hist_n) CUDA_TRY(cudaMemcpyAsync(hist_out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (n_frames)
     CUDA_TRY(cudaMemcpyAsync(fld_out, d_fld.p, (size_t)n * n_frames * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -788,7 +852,7 @@ int bfe_run_v5(bfe_plan* plan, int64_t n_t, const double* time,
   CUDA_TRY(cudaStreamSynchronize(st));
   if (n_frames) std::memcpy(fld_time_out, ftime.data(), n_frames * sizeof(double));
   if (dev != plan->device) cudaSetDevice(dev);
-  return BFE_OK;
+  return xrc;
 } catch (...) {
   return bfe::exception_status();
 }

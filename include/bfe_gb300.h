@@ -39,10 +39,15 @@ extern "C" {
 #define BFE_ERR_ARG 1          /* invalid argument (sizes, indices, strings) */
 #define BFE_ERR_OOM 2          /* host or device allocation failed */
 #define BFE_ERR_CUDA 3         /* CUDA runtime error */
-#define BFE_ERR_NUMERIC 4      /* zero lumped mass, NaN/Inf in K, C or M (non-finite signals
-                                  propagate into the outputs, as in the reference) */
+#define BFE_ERR_NUMERIC 4      /* zero lumped mass, NaN/Inf in K, C or M */
 #define BFE_ERR_UNSUPPORTED 5  /* valid request the reference path rejects */
 #define BFE_ERR_NO_DEVICE 6    /* no usable GPU */
+#define BFE_ERR_UNSTABLE 7     /* the march produced non-finite values: a time step above the
+                                  stability limit, or non-finite forcing signals. The outputs
+                                  are still written as computed (the reference returns the same
+                                  NaN/Inf values with no error) */
+#define BFE_ERR_TIMEOUT 8      /* the run exceeded the plan's time limit (bfe_plan_set_time_limit);
+                                  the outputs hold the samples computed before it stopped */
 
 /* sparse matrix storage formats */
 #define BFE_CSR 0              /* ptr = row pointers, idx = column indices  */
@@ -404,6 +409,17 @@ typedef struct bfe_stats {
 
 /* Enable (1) or disable (0) CUDA-event timing of every launch in later runs. */
 int bfe_plan_set_timing(bfe_plan* plan, int32_t enable);
+
+/*
+ * Wall-clock limit of later runs on this plan, in seconds (0 = none, the
+ * default; no reference counterpart: MATLAB's loop at
+ * fn_explicit_dynamic_solver_v6.m:180-218 runs to the end). With a limit,
+ * the host checks the clock between chunks of 48 time steps while keeping
+ * one chunk queued ahead on the GPU; once the limit has passed it launches
+ * no further steps, waits for the launched ones, copies the outputs computed
+ * so far and returns BFE_ERR_TIMEOUT. The plan stays usable.
+ */
+int bfe_plan_set_time_limit(bfe_plan* plan, double seconds);
 
 /* Copy the counters of the plan's last run. */
 int bfe_plan_stats(const bfe_plan* plan, bfe_stats* out);

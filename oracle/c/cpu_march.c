@@ -35,6 +35,10 @@ int cpu_threads(void) {
  *   interface rows: n_int rows int_row[], CSR pi_ptr/pi_col/pi_val of P^-1 rows
  *   forcing: n_frc entries (row, sig) with signals sig[ti * n_sig + k]
  *   hist: q x n_t (column-major) for one right-hand side
+ *   frames (v6.m:200-208): every_n > 0 writes frame k = ti / every_n at the
+ *   samples ti = 0, every_n, 2 every_n, ... (MATLAB's 1:every:n_t) into
+ *   fld (n x n_frames, column-major) as (u - u_prev) / dt when field_is_vel,
+ *   else u, and its time into fld_time; frames before ti_start stay zero
  */
 int cpu_march(int64_t n, const int64_t* b_ptr, const int64_t* b_col, const double* b_val,
               const int64_t* d_ptr, const int64_t* d_col, const double* d_val,
@@ -43,7 +47,9 @@ int cpu_march(int64_t n, const int64_t* b_ptr, const int64_t* b_col, const doubl
               const int64_t* pi_col, const double* pi_val,
               int64_t n_t, int64_t ti_start, int64_t n_frc, const int64_t* frc_row,
               const int64_t* frc_sig, int64_t n_sig, const double* sig,
-              int64_t q, const int64_t* hist_idx, double* hist) {
+              int64_t q, const int64_t* hist_idx, double* hist,
+              int64_t every_n, int32_t field_is_vel, double dt, const double* time,
+              double* fld, double* fld_time) {
   double* u0 = (double*)calloc((size_t)n, sizeof(double));
   double* u1 = (double*)calloc((size_t)n, sizeof(double));
   double* u2 = (double*)calloc((size_t)n, sizeof(double));
@@ -72,6 +78,12 @@ int cpu_march(int64_t n, const int64_t* b_ptr, const int64_t* b_col, const doubl
       u0[int_row[t]] = acc;
     }
     for (int64_t k = 0; k < q; ++k) hist[k + q * ti] = u0[hist_idx[k]];
+    if (every_n > 0 && fld && ti % every_n == 0) {
+      double* col = fld + (size_t)n * (size_t)(ti / every_n);
+      fld_time[ti / every_n] = time[ti];
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) col[i] = field_is_vel ? (u0[i] - u1[i]) / dt : u0[i];
+    }
     double* tmp = u2; u2 = u1; u1 = u0; u0 = tmp;
   }
   free(u0); free(u1); free(u2); free(r); free(f); free(is_int);

@@ -78,8 +78,12 @@ class CpuOperator:
         self.irows = irows
         self.Pi = Pi.tocsr()
 
-    def march(self, time, frc_idx0, F, hist_idx0):
-        """FP64 march of one source (0-based indices). F: (rows, n_t), rows 1 or p."""
+    def march(self, time, frc_idx0, F, hist_idx0, every_n=0, field_is_vel=True, frames=False):
+        """FP64 march of one source (0-based indices). F: (rows, n_t), rows 1 or p.
+
+        Returns the q x n_t history; with frames=True returns (hist, fld,
+        fld_time), fld n x n_frames holding a frame every every_n samples
+        from the first (fn_explicit_dynamic_solver_v6.m:200-208)."""
         lib = _load()
         nt = len(time)
         F = np.atleast_2d(np.asarray(F, float))
@@ -96,6 +100,12 @@ class CpuOperator:
         hist_idx0 = np.asarray(hist_idx0, np.int64)
         q = hist_idx0.size
         hist = np.zeros((q, nt), order="F")
+        every = int(every_n) if (frames and every_n and every_n > 0) else 0
+        nf = (nt + every - 1) // every if every else 0
+        fld = np.zeros((self.n, nf), order="F")
+        fld_t = np.zeros(nf)
+        tm = np.ascontiguousarray(np.asarray(time, float))
+        dt = float(tm[1] - tm[0]) if nt > 1 else 1.0
 
         def P(a, t):
             return a.ctypes.data_as(ctypes.POINTER(t))
@@ -110,10 +120,12 @@ class CpuOperator:
             P(self.acoef, cd), P(self.pinv, cd),
             c64(self.irows.size), P(self.irows, c64), P(arrs[6], c64), P(arrs[7], c64), P(arrs[8], cd),
             c64(nt), c64(ti0), c64(rows.size), P(rows, c64), P(sigk, c64), c64(sig.shape[1]),
-            P(sig, cd), c64(q), P(hist_idx0, c64), P(hist, cd))
+            P(sig, cd), c64(q), P(hist_idx0, c64), P(hist, cd),
+            c64(every), ctypes.c_int32(1 if field_is_vel else 0), cd(dt), P(tm, cd),
+            P(fld, cd) if every else None, P(fld_t, cd) if every else None)
         if st != 0:
             raise RuntimeError("cpu_march failed")
-        return hist
+        return (hist, fld, fld_t) if frames else hist
 
 
 def time_march(op, time, frc_idx0, F, hist_idx0, min_seconds=0.0):

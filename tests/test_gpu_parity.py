@@ -60,7 +60,7 @@ def test_solid_plate_history_and_frames(bfe, plate, prec, tol):
     assert frc is None
     assert h1.shape == h0.shape and f1.shape == f0.shape
     assert _err(h1, h0) <= tol
-    assert _err(f1, f0) <= tol * 10
+    assert _err(f1, f0) <= tol
     assert np.array_equal(ft1, ft0)
 
 
