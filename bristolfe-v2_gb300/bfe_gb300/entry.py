@@ -57,6 +57,17 @@ def nds_and_dfs_to_gi(nds, dfs, gl_lookup):
     return gi[valid], nds[valid], dfs[valid], valid
 
 
+def _mask_rows(a, mask):
+    """a(mask, :) with MATLAB's logical indexing: a mask shorter than the
+    rows selects among the first rows (fn_BristolFE_v2.m:82-84 applies a
+    step's validity mask to forces that steps{1}.load.wts may have given
+    more rows); a true beyond the last row is an index error."""
+    idx = np.nonzero(np.asarray(mask, bool).ravel())[0]
+    if idx.size and idx.max() >= a.shape[0]:
+        raise IndexError("logical index exceeds the %d rows" % a.shape[0])
+    return a[idx]
+
+
 def _grow_rows(valid, values, nt):
     """res.dsps(valid, :) = values on an unset field (fn_BristolFE_v2.m:127):
     the array grows to the last valid row."""
@@ -163,11 +174,11 @@ def fn_BristolFE_v2_gb300(mod, matls, steps, fe_options=None):
         if "frcs" in load:
             job["frc_gi"], _, _, valid_f = nds_and_dfs_to_gi(load["frc_nds"], load["frc_dfs"], gl)
             frcs = _weighted(steps, np.atleast_2d(np.asarray(load["frcs"], float)))
-            job["frcs"] = frcs[valid_f] if frcs.shape[0] > 1 else frcs
+            job["frcs"] = _mask_rows(frcs, valid_f) if frcs.shape[0] > 1 else frcs
         if "dsps" in load:
             job["dsp_gi"], _, _, r["valid_appl_dsps"] = nds_and_dfs_to_gi(load["dsp_nds"], load["dsp_dfs"], gl)
             dsps = _weighted(steps, np.atleast_2d(np.asarray(load["dsps"], float)))
-            job["dsps"] = dsps[r["valid_appl_dsps"]] if dsps.shape[0] > 1 else dsps
+            job["dsps"] = _mask_rows(dsps, r["valid_appl_dsps"]) if dsps.shape[0] > 1 else dsps
         mon = st.get("mon", {})
         job["has_mon"] = "nds" in mon
         if job["has_mon"]:

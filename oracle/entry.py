@@ -33,6 +33,17 @@ def nds_and_dfs_to_gi(nds, dfs, gl_lookup):
     return gi[valid], nds[valid], dfs[valid], valid
 
 
+def _mask_rows(a, mask):
+    """a(mask, :) with MATLAB's logical indexing: a mask shorter than the
+    rows selects among the first rows (fn_BristolFE_v2.m:82-84 applies a
+    step's validity mask to forces that steps{1}.load.wts may have given
+    more rows); a true beyond the last row is an index error."""
+    idx = np.nonzero(np.asarray(mask, bool).ravel())[0]
+    if idx.size and idx.max() >= a.shape[0]:
+        raise IndexError("logical index exceeds the %d rows" % a.shape[0])
+    return a[idx]
+
+
 def _grow_rows(valid, values, nt):
     """res.dsps(valid, :) = values on an unset field (fn_BristolFE_v2.m:127):
     MATLAB sizes the new array to the last true index of the mask."""
@@ -71,7 +82,7 @@ def BristolFE_v2(mod, matls, steps, fe_options=None):
             if "wts" in steps[0]["load"]:              # steps{1} used for all (:79)
                 frcs = np.asarray(steps[0]["load"]["wts"], float).reshape(-1, 1) @ frcs
             if frcs.shape[0] > 1:
-                frcs = frcs[valid_f]
+                frcs = _mask_rows(frcs, valid_f)
         else:
             frc_gi, frcs = np.zeros(0, np.int64), None
         dsp_gi, dsps = np.zeros(0, np.int64), None
@@ -81,7 +92,7 @@ def BristolFE_v2(mod, matls, steps, fe_options=None):
             if "wts" in steps[0]["load"]:
                 dsps = np.asarray(steps[0]["load"]["wts"], float).reshape(-1, 1) @ dsps
             if dsps.shape[0] > 1:
-                dsps = dsps[r["valid_appl_dsps"]]
+                dsps = _mask_rows(dsps, r["valid_appl_dsps"])
         mon = st.get("mon", {})
         if "nds" in mon:
             hist_gi, _, _, r["valid_mon_dsps"] = nds_and_dfs_to_gi(mon["nds"], mon["dfs"], gl)
