@@ -22,3 +22,8 @@ double mxGetScalar(const mxArray*);
 int mxIsInf(double);
 mxArray* mxCreateDoubleMatrix(mwSize, mwSize, mxComplexity);
 int mexAtExit(void (*)(void));
+typedef enum { mxDOUBLE_CLASS = 6, mxSINGLE_CLASS = 7 } mxClassID;
+typedef float mxSingle;
+mxArray* mxCreateNumericMatrix(mwSize, mwSize, mxClassID, mxComplexity);
+mxSingle* mxGetSingles(const mxArray*);
+void mxFree(void*);
