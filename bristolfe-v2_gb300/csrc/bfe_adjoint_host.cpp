@@ -28,6 +28,11 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   if (!pl) return fail(BFE_ERR_ARG, "plan is NULL");
   if (pl->mode != BFE_MODE_VEL_CURRENT)
     return fail(BFE_ERR_UNSUPPORTED, "the adjoint is defined for 'vel at curent time step'");
+  // the backward sweep applies P^-1 as a diagonal; fluid-solid coupling in C
+  // (ASI2D2, fn_el_ASI2D2.m:61-76) makes P non-diagonal on the interface rows
+  if (pl->n_int > 0)
+    return fail(BFE_ERR_UNSUPPORTED, "the adjoint needs a diagonal P: this plan has %d fluid-solid interface "
+                "rows (off-diagonal C)", (int)pl->n_int);
   if (n_el < 1 || !bfe::grad_ndf_supported(ndf) || !el_dof || !ke || !mh || !ch)
     return fail(BFE_ERR_ARG, "invalid element data (ndf must be 3, 6, 8, 9 or 24)");
   if (R < 1 || q < 1 || !hist_idx || !observed || !misfit || !g_stiff || !g_rho)

@@ -379,7 +379,14 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
  * its checkpoint, steps the adjoint through it and contracts the segment
  * into the gradients in one pass. Device memory: about 2 n R (steps / c
  * + c) state values for c = ckpt_every (checkpoints, and the segment's
- * forward and adjoint states). Only 'vel at curent time step' plans.
+ * forward and adjoint states). Only 'vel at curent time step' plans with a
+ * diagonal P: a plan with fluid-solid interface rows (off-diagonal C from
+ * ASI2D2 elements) returns BFE_ERR_UNSUPPORTED.
+ * For solid elements (CPE3, bricks) M and C scale with the density, so
+ * g_rho is dJ/drho. Acoustic elements (AC2D3, fn_el_AC2D3.m:59-77) have a
+ * mass that scales with 1/bulk modulus and a stiffness that scales with
+ * 1/rho: for them g_rho is the derivative with respect to the factor
+ * multiplying mh and ch, and g_stiff the one multiplying ke.
  * hist_out (optional) receives the forward A-scans.
  */
 int bfe_adjoint_gradient(bfe_plan* plan, int64_t n_el, int32_t ndf, const int64_t* el_dof,

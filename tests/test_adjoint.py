@@ -299,3 +299,25 @@ def test_one_dof_triangle_adjoint_matches_oracle(bfe, prec, R, tol):
     assert abs(J1 - J0) <= tol * J0
     assert np.abs(gs1 - gs0).max() <= tol * np.abs(gs0).max()
     assert np.abs(gr1 - gr0).max() <= tol * np.abs(gr0).max()
+
+
+def test_plans_with_fluid_solid_interface_rows_are_rejected(bfe):
+    """A coupled water/steel plan: ASI2D2 puts the fluid-solid coupling in C
+    (fn_el_ASI2D2.m:61-76), so P is not diagonal on the interface rows and
+    the adjoint returns BFE_ERR_UNSUPPORTED instead of a wrong gradient."""
+    from bfe_gb300 import _lib
+    m = modelgen.coupled_model(W=2e-3, Hw=1e-3, Hs=1e-3, h=0.1e-3, abs_thick=0.3e-3)
+    n = m["K"].shape[0]
+    nt = 60
+    t = np.arange(nt) * m["dt"]
+    sig = signals.gaussian_pulse(t, 5e6, 5)
+    src = [modelgen.gi_of(m["gl"], [m["frc_nd"]], 4)]
+    hi = modelgen.gi_of(m["gl"], m["mon_nds"], 4)
+    dof = np.arange(3 * (n // 3), dtype=np.int64).reshape(-1, 3)
+    ke = np.zeros((dof.shape[0], 3, 3))
+    mh = np.ones((dof.shape[0], 3))
+    with bfe.Plan(m["K"], m["C"], m["M"], m["dt"], bfe.VEL_CURRENT, "double") as plan:
+        with pytest.raises(bfe.BfeError) as ei:
+            plan.adjoint_gradient((ke, mh, 0 * mh, dof), t, src, sig, hi, np.zeros((hi.size, nt, 1)))
+    assert ei.value.status == _lib.BFE_ERR_UNSUPPORTED
+    assert "interface" in str(ei.value)
