@@ -35,7 +35,7 @@ struct alignas(sizeof(T) * VEC) Pack {
   T v[VEC];
 };
 
-// read-only load of VEC consecutive values (16-byte aligned when VEC > 1)
+// read-only load of VEC consecutive values (aligned to the pack's size)
 template <typename T, int VEC>
 __device__ __forceinline__ Pack<T, VEC> ld_pack(const T* p) {
   Pack<T, VEC> r;
@@ -44,8 +44,11 @@ __device__ __forceinline__ Pack<T, VEC> ld_pack(const T* p) {
   } else if constexpr (sizeof(T) == 4 && VEC == 4) {
     const float4 x = __ldg(reinterpret_cast<const float4*>(p));
     r.v[0] = x.x; r.v[1] = x.y; r.v[2] = x.z; r.v[3] = x.w;
+  } else if constexpr (sizeof(T) == 4 && VEC == 2) {
+    const float2 x = __ldg(reinterpret_cast<const float2*>(p));
+    r.v[0] = x.x; r.v[1] = x.y;
   } else {
-    static_assert(sizeof(T) == 8 && VEC == 2, "16-byte packs only");
+    static_assert(sizeof(T) == 8 && VEC == 2, "8- or 16-byte packs only");
     const double2 x = __ldg(reinterpret_cast<const double2*>(p));
     r.v[0] = x.x; r.v[1] = x.y;
   }
@@ -158,6 +161,79 @@ __global__ void __launch_bounds__(256) grad_stiff(int64_t n_el, const int32_t* _
   if (sub == 0) gs[e] -= scale * a;
 }
 
+// dJ/ds with the element stiffness factored on the host as K_e = W_e W_e^T
+// (W_e: NDF x RK, a pivoted Cholesky; RK is the element's rank):
+//   lam' K_e u = (W_e' lam) . (W_e' u)
+// 2 NDF RK + RK multiply-adds per element and source instead of NDF^2 + NDF,
+// and W_e takes NDF RK registers instead of NDF^2. Elements arrive sorted by
+// their lowest DOF row, so the groups of a warp gather neighbouring node rows
+// and every row is fetched from DRAM about once per step; the sums go to the
+// element's original slot el_out[e].
+template <typename T, int NDF, int RK, int VEC>
+__global__ void __launch_bounds__(256) grad_stiff_w(int64_t n_el, const int32_t* __restrict__ el_dof,
+                                                    const T* __restrict__ w, const int32_t* __restrict__ el_out,
+                                                    const T* __restrict__ lam, const T* __restrict__ u,
+                                                    int64_t stride, int n_steps, int R, int tpe, double scale,
+                                                    double* __restrict__ gs) {
+  using P = Pack<T, VEC>;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t e = gt / tpe;
+  const int sub = (int)(gt % tpe);
+  if (e >= n_el) return;       // whole groups leave together: tpe divides 32 and the block size
+  const int lane = threadIdx.x & 31;
+  const unsigned mask = tpe == 32 ? 0xffffffffu : ((1u << tpe) - 1u) << (lane & ~(tpe - 1));
+  int32_t dof[NDF];
+  T W[NDF][RK];
+#pragma unroll
+  for (int i = 0; i < NDF; ++i) {
+    dof[i] = __ldg(el_dof + e * NDF + i);
+#pragma unroll
+    for (int q = 0; q < RK; ++q) W[i][q] = __ldg(w + (e * NDF + i) * RK + q);
+  }
+  const int nv = R / VEC;
+  StepSum<T> acc;
+  for (int k = 0; k < n_steps; ++k) {
+    const T* L = lam + (size_t)k * stride;          // lam_t
+    const T* U1 = u + (size_t)(k + 1) * stride;     // u_{t-1}
+    for (int cv = sub; cv < nv; cv += tpe) {
+      const size_t r = (size_t)cv * VEC;
+      T y[RK][VEC], z[RK][VEC];
+#pragma unroll
+      for (int q = 0; q < RK; ++q)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) y[q][v] = z[q][v] = T(0);
+#pragma unroll
+      for (int j = 0; j < NDF; ++j) {
+        const bool use = dof[j] >= 0;
+        const size_t o = (size_t)(use ? dof[j] : 0) * R + r;
+        P a = ld_pack<T, VEC>(U1 + o);
+        P l = ld_pack<T, VEC>(L + o);
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) {
+          a.v[v] = use ? a.v[v] : T(0);
+          l.v[v] = use ? l.v[v] : T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < RK; ++q)
+#pragma unroll
+          for (int v = 0; v < VEC; ++v) {
+            y[q][v] = fma(W[j][q], a.v[v], y[q][v]);
+            z[q][v] = fma(W[j][q], l.v[v], z[q][v]);
+          }
+      }
+      T ss = T(0);
+#pragma unroll
+      for (int q = 0; q < RK; ++q)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) ss = fma(y[q][v], z[q][v], ss);
+      acc.add(ss);
+    }
+  }
+  double a = acc.value();
+  for (int off = tpe >> 1; off > 0; off >>= 1) a += __shfl_xor_sync(mask, a, off);
+  if (sub == 0) gs[__ldg(el_out + e)] -= scale * a;
+}
+
 // dJ/drho, per DOF: mh and ch are constant in time, so the density term
 // needs only, per DOF d and summed over the steps and sources,
 //   pw[d] += lam_t[d] (u_t - 2 u_{t-1} + u_{t-2})[d]
@@ -254,16 +330,48 @@ cudaError_t launch_stiff(const GradArgs& g, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// sources per lane of the factored pass: 2 (8 bytes) keeps the per-source
+// sums and loads in flight within the register budget of 24 warps per SM
+template <typename T, int NDF, int RK>
+cudaError_t launch_stiff_w(const GradArgs& g, cudaStream_t st) {
+  constexpr int VMAX = sizeof(T) == 4 ? 2 : 1;
+  const int vec = g.R % VMAX == 0 ? VMAX : 1;
+  const int tpe = lanes_for(g.R, vec);
+  const int threads = 256;
+  const int64_t blocks = (g.n_el * tpe + threads - 1) / threads;
+  if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+  const T* w = static_cast<const T*>(g.w);
+  const T* l = static_cast<const T*>(g.lam);
+  const T* u = static_cast<const T*>(g.u);
+  const double scale = g.dt * g.dt;
+  if (vec == VMAX && VMAX > 1)
+    grad_stiff_w<T, NDF, RK, VMAX><<<(unsigned)blocks, threads, 0, st>>>(
+        g.n_el, g.el_dof_w, w, g.el_out, l, u, g.stride, g.n_steps, g.R, tpe, scale, g.gs);
+  else
+    grad_stiff_w<T, NDF, RK, 1><<<(unsigned)blocks, threads, 0, st>>>(
+        g.n_el, g.el_dof_w, w, g.el_out, l, u, g.stride, g.n_steps, g.R, tpe, scale, g.gs);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_grad_t(const GradArgs& g, cudaStream_t st) {
   cudaError_t e;
-  switch (g.ndf) {
-    case 3: e = launch_stiff<T, 3>(g, st); break;
-    case 6: e = launch_stiff<T, 6>(g, st); break;
-    case 8: e = launch_stiff<T, 8>(g, st); break;
-    case 9: e = launch_stiff<T, 9>(g, st); break;
-    case 24: e = launch_stiff<T, 24>(g, st); break;
-    default: return cudaErrorInvalidValue;
+  if (g.w) {
+    switch (g.ndf) {
+      case 3: e = launch_stiff_w<T, 3, 2>(g, st); break;
+      case 6: e = launch_stiff_w<T, 6, 3>(g, st); break;
+      case 9: e = launch_stiff_w<T, 9, 5>(g, st); break;
+      default: return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (g.ndf) {
+      case 3: e = launch_stiff<T, 3>(g, st); break;
+      case 6: e = launch_stiff<T, 6>(g, st); break;
+      case 8: e = launch_stiff<T, 8>(g, st); break;
+      case 9: e = launch_stiff<T, 9>(g, st); break;
+      case 24: e = launch_stiff<T, 24>(g, st); break;
+      default: return cudaErrorInvalidValue;
+    }
   }
   if (e != cudaSuccess) return e;
   constexpr int VMAX = (int)(16 / sizeof(T));
@@ -285,6 +393,8 @@ cudaError_t launch_grad_t(const GradArgs& g, cudaStream_t st) {
 }  // namespace
 
 bool grad_ndf_supported(int ndf) { return ndf == 3 || ndf == 6 || ndf == 8 || ndf == 9 || ndf == 24; }
+
+int grad_factor_rank(int ndf) { return ndf == 3 ? 2 : ndf == 6 ? 3 : ndf == 9 ? 5 : 0; }
 
 cudaError_t launch_grad(const GradArgs& g, int precision, cudaStream_t st) {
   if (g.n_steps < 1) return cudaSuccess;

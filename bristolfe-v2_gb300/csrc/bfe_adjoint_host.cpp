@@ -5,6 +5,44 @@
 
 using namespace bfe_host;
 
+namespace {
+
+// Pivoted Cholesky K = W W^T of a symmetric positive semi-definite element
+// matrix (outer-product form, largest remaining diagonal first, pivots below
+// 1e-13 of the largest diagonal end it). W is ndf x rk, row-major,
+// zero-padded. Returns the rank, or -1 when the matrix is not positive
+// semi-definite (a residual above 1e-11 of the largest diagonal remains) or
+// its rank exceeds rk.
+int factor_psd(double* A, int ndf, int rk, double* W) {
+  double d0 = 0.0;
+  for (int i = 0; i < ndf; ++i) d0 = std::max(d0, std::fabs(A[i * ndf + i]));
+  std::fill(W, W + ndf * rk, 0.0);
+  if (d0 == 0.0) {
+    for (int i = 0; i < ndf * ndf; ++i)
+      if (A[i] != 0.0) return -1;
+    return 0;
+  }
+  int r = 0;
+  for (;;) {
+    int p = -1;
+    double best = 1e-13 * d0;
+    for (int i = 0; i < ndf; ++i)
+      if (A[i * ndf + i] > best) { best = A[i * ndf + i]; p = i; }
+    if (p < 0) break;
+    if (r == rk) return -1;
+    const double sc = 1.0 / std::sqrt(A[p * ndf + p]);
+    for (int i = 0; i < ndf; ++i) W[i * rk + r] = A[i * ndf + p] * sc;
+    for (int i = 0; i < ndf; ++i)
+      for (int j = 0; j < ndf; ++j) A[i * ndf + j] -= W[i * rk + r] * W[j * rk + r];
+    ++r;
+  }
+  for (int i = 0; i < ndf * ndf; ++i)
+    if (std::fabs(A[i]) > 1e-11 * d0) return -1;
+  return r;
+}
+
+}  // namespace
+
 extern "C" {
 
 // Adjoint gradient of an A-scan misfit with sqrt(N)-step checkpointing (see
@@ -72,6 +110,53 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
     CUDA_TRY(d_ke.upload(cast_bytes(prec, ke, n_el * ndf * ndf)));
     CUDA_TRY(d_mh.upload(cast_bytes(prec, mh, n_el * ndf)));
     CUDA_TRY(d_ch.upload(cast_bytes(prec, ch, n_el * ndf)));
+  }
+  // The stiffness pass of the contraction takes K_e = W_e W_e^T (unused DOFs'
+  // rows and columns zeroed first) with the elements sorted by their lowest
+  // DOF row; when an element is not positive semi-definite or its rank is
+  // above what the pass is compiled for, every element keeps K_e.
+  DevBuf<int32_t> d_dof_w, d_out;
+  DevBuf<unsigned char> d_w;
+  const int rk = bfe::grad_factor_rank(ndf);
+  bool factored = false;
+  if (rk > 0) {
+    std::vector<double> W((size_t)n_el * ndf * rk);
+    std::atomic<bool> ok{true};
+    const int nth = plan_threads(n_el, 8192);
+    const bool done = parallel_chunks(n_el, nth, [&](int, int64_t b, int64_t e_end) {
+      std::vector<double> A((size_t)ndf * ndf);
+      for (int64_t e = b; e < e_end && ok; ++e) {
+        for (int i = 0; i < ndf; ++i)
+          for (int j = 0; j < ndf; ++j) {
+            const bool use = el_dof[e * ndf + i] >= 0 && el_dof[e * ndf + j] >= 0;
+            A[i * ndf + j] = use ? ke[(e * ndf + i) * ndf + j] : 0.0;
+          }
+        if (factor_psd(A.data(), ndf, rk, W.data() + (size_t)e * ndf * rk) < 0) ok = false;
+      }
+    });
+    if (done && ok) {
+      std::vector<int64_t> key(n_el);
+      for (int64_t e = 0; e < n_el; ++e) {
+        int64_t k = INT64_MAX;
+        for (int i = 0; i < ndf; ++i)
+          if (el_dof[e * ndf + i] >= 0) k = std::min<int64_t>(k, el_dof[e * ndf + i]);
+        key[e] = k;
+      }
+      std::vector<int32_t> ord(n_el);
+      std::iota(ord.begin(), ord.end(), 0);
+      std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+      std::vector<int32_t> dof_w((size_t)n_el * ndf);
+      std::vector<double> w_sorted((size_t)n_el * ndf * rk);
+      for (int64_t k = 0; k < n_el; ++k) {
+        const int64_t e = ord[k];
+        for (int i = 0; i < ndf; ++i) dof_w[k * ndf + i] = (int32_t)el_dof[e * ndf + i];
+        std::copy(W.begin() + e * ndf * rk, W.begin() + (e + 1) * ndf * rk, w_sorted.begin() + k * ndf * rk);
+      }
+      CUDA_TRY(d_dof_w.upload(dof_w));
+      CUDA_TRY(d_out.upload(ord));
+      CUDA_TRY(d_w.upload(cast_bytes(prec, w_sorted.data(), n_el * ndf * rk)));
+      factored = true;
+    }
   }
   // forward inputs
   const int64_t n_sig = frc_rows * R;
@@ -199,6 +284,11 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   g.n = n;
   g.pw = d_pw.p;
   g.pv = d_pv.p;
+  if (factored) {
+    g.w = d_w.p;
+    g.el_dof_w = d_dof_w.p;
+    g.el_out = d_out.p;
+  }
   for (int64_t j = n_seg - 1; j >= 0; --j) {
     const int64_t ts = ti0 + j * c, te = std::min(ts + c, n_t);
     CUDA_TRY(cudaMemcpyAsync(S(0), d_ck.p + 2 * sb * j, 2 * sb, cudaMemcpyDeviceToDevice, st));

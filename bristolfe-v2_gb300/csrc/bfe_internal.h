@@ -261,8 +261,18 @@ struct GradArgs {
   double* gr;                 // dJ/drho accumulators (n_el)
   double* pw;                 // per-DOF sums of lam_t (u_t - 2 u_{t-1} + u_{t-2}) (n)
   double* pv;                 // per-DOF sums of lam_t (u_t - u_{t-2}) (n)
+  // factored stiffness K_e = W_e W_e^T (nullptr: the stiffness pass uses ke):
+  // elements in traversal order (sorted by their lowest DOF row, so that
+  // elements sharing nodes run together), W_e as ndf x grad_factor_rank(ndf)
+  const void* w;
+  const int32_t* el_dof_w;    // n_el x ndf rows, traversal order
+  const int32_t* el_out;      // original index of each element in traversal order
 };
 bool grad_ndf_supported(int ndf);
+// Columns of the factored element stiffness the stiffness pass is compiled
+// for (0: no factored pass for this ndf): 2 for 3-DOF scalar triangles, 3 for
+// 6-DOF plane-strain triangles, 5 for 9-DOF ones.
+int grad_factor_rank(int ndf);
 // one segment: gs and the per-DOF sums pw, pv
 cudaError_t launch_grad(const GradArgs& g, int precision, cudaStream_t s);
 // after the last segment: gr from pw, pv
