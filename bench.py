@@ -147,14 +147,10 @@ def measured_peak_hbm():
 
 
 KERNEL_NAMES = {
-    0: "step_batched<float,2> (slice-staged rows)", 1: "step_f32_x64<4,4>", 2: "step_f32_x64<4,3>",
-    3: "step_f32_x64<8,2>", 4: "step_f32_node<3,8>", 5: "step_f32_node<3,12>",
-    6: "step_f32_group<2>", 7: "step_f32_group<4>", 8: "step_f32_group_async",
+    0: "step_batched<float,2> (slice-staged rows)",
     9: "step_f32_group2<2,1,1>", 10: "step_f32_group2<2,2,1>", 11: "step_f32_group2<2,4,1>",
     12: "step_f32_group2<2,1,4>", 13: "step_f32_group2<2,1,6>", 14: "step_f32_group2<2,1,8>",
-    15: "step_f32_group_tma", 16: "step_f32_group4<1,10>", 17: "step_f32_group4<2,8>",
-    18: "step_f32_group4<1,12>", 19: "step_f32_group4<1,12,late>", 20: "step_f32_group4<1,12,raw>",
-    21: "step_f32_group4<1,12,late,raw>", 22: "step_f32_group4<1,10,raw>",
+    20: "step_f32_group4<12>", 22: "step_f32_group4<10>",
 }
 
 

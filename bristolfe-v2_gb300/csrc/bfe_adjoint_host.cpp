@@ -179,19 +179,18 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   const bool use_groups = pl->have_groups && (prec == BFE_PREC_SINGLE ? (R % 64 == 0 || R == 16 || R == 32)
                                                                        : R % 16 == 0);
   const bfe::GroupArgs* grp = use_groups ? &pl->groups : nullptr;
-  // the variant the forward runs chose for this R, else the half-warp kernel
-  // (FP32: raw coefficients, 3D plans map it to the warp-per-node kernel;
-  // FP64: the widest group form R allows)
-  int variant = !use_groups ? 0 : prec == BFE_PREC_SINGLE ? 20 : (R % 64 == 0 ? 1 : R % 32 == 0 ? 2 : 3);
-  if (use_groups) {
+  // the variant the forward runs chose for this R, else the default candidate
+  int variant = 0;
+  if (R > 1) {
+    int cand[8];
+    bfe::batched_candidates(prec, (int)R, use_groups, grp ? bfe::group_max_bs(*grp) : 0, cand);
+    variant = cand[0];
     auto it = pl->variant_of_R.find(R);
-    // the TMA variant needs tensor maps of the march's state buffers, which
-    // the adjoint's slot buffers do not have: it takes the default kernel
-    if (it != pl->variant_of_R.end() && it->second != 15) variant = it->second;
+    if (it != pl->variant_of_R.end()) variant = it->second;
   }
   auto step = [&](bfe::StepArgs& a) -> int {
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, nullptr, grp, prec, pl->max_slice_entries, variant, st);
+                           : bfe::launch_step_batched(a, grp, prec, pl->max_slice_entries, variant, st);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (pl->n_int) {
       e = bfe::launch_interface_fixup(a, prec, st);

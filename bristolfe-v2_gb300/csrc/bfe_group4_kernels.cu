@@ -12,11 +12,9 @@ namespace bfe {
 
 // Group block-sparse kernel with a half-warp per node: each lane carries four
 // right-hand sides (float4), so every load, address and index instruction
-// serves two nodes, and a warp holds two nodes' work at the cost of one.
-// UNROLL neighbours are loaded before they are used; LATE_UP reads u_{n-1}
-// only in the epilogue (fewer live registers); RAW reads a 2 x 2 block's
-// coefficients with one 16-byte load of the plain [k][l] array and forms the
-// broadcast pairs in registers (half the coefficient bytes and loads).
+// serves two nodes, and a warp holds two nodes' work at the cost of one. A
+// 2 x 2 block's coefficients come with one 16-byte load of the plain [k][l]
+// array and become broadcast pairs in registers.
 __device__ __forceinline__ float4 f4sub(float4 a, float4 b) {
   const float2 lo = f2sub(make_float2(a.x, a.y), make_float2(b.x, b.y));
   const float2 hi = f2sub(make_float2(a.z, a.w), make_float2(b.z, b.w));
@@ -29,31 +27,22 @@ __device__ __forceinline__ float4 f4fma(float2 c, float4 x, float4 acc) {   // c
 }
 
 // One neighbour block of a node: acc_k += sum_l c_kl (u_own_l - u_nbr_l).
-template <int BS, bool RAW>
-__device__ __forceinline__ void group4_nbr(const float* nb, const float2* coef, const float* craw, int e,
-                                           size_t rs, const float4 (&uo)[BS], float4 (&acc)[BS]) {
+template <int BS>
+__device__ __forceinline__ void group4_nbr(const float* nb, const float* craw, int e, size_t rs,
+                                           const float4 (&uo)[BS], float4 (&acc)[BS]) {
   float4 g[BS];
 #pragma unroll
   for (int l = 0; l < BS; ++l) g[l] = __ldg(reinterpret_cast<const float4*>(nb + l * rs));
   float2 cv[BS * BS];
-  if (RAW && BS == 2) {
+  if (BS == 2) {
     const float4 cr = __ldg(reinterpret_cast<const float4*>(craw + (size_t)e * 4));
     cv[0] = make_float2(cr.x, cr.x);
     cv[1] = make_float2(cr.y, cr.y);
     cv[2 % (BS * BS)] = make_float2(cr.z, cr.z);
     cv[3 % (BS * BS)] = make_float2(cr.w, cr.w);
-  } else if (RAW) {
+  } else {
     const float cr = __ldg(craw + e);
     cv[0] = make_float2(cr, cr);
-  } else if (BS == 2) {
-    const float4 c0 = __ldg(reinterpret_cast<const float4*>(coef + (size_t)e * 4));
-    const float4 c1 = __ldg(reinterpret_cast<const float4*>(coef + (size_t)e * 4 + 2));
-    cv[0] = make_float2(c0.x, c0.y);
-    cv[1] = make_float2(c0.z, c0.w);
-    cv[2 % (BS * BS)] = make_float2(c1.x, c1.y);
-    cv[3 % (BS * BS)] = make_float2(c1.z, c1.w);
-  } else {
-    cv[0] = __ldg(coef + e);
   }
 #pragma unroll
   for (int l = 0; l < BS; ++l) {
@@ -103,7 +92,6 @@ __device__ __forceinline__ void finish4(const StepArgs& a, int row, int c, float
 // One-DOF (fluid) node with 8 lanes: each lane carries the right-hand sides
 // c .. c + 3 and c + 32 .. c + 35, so a neighbour's index and coefficient
 // serve 512 bytes of state as in the two-DOF form.
-template <int UNROLL, bool RAW>
 __device__ __forceinline__ void group4_fluid(const StepArgs& a, const GroupArgs& gr, int gi, int node, int l8) {
   const int4 rec = __ldg(gr.rec[gi] + node);
   const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
@@ -111,21 +99,19 @@ __device__ __forceinline__ void group4_fluid(const StepArgs& a, const GroupArgs&
   const size_t rs = (size_t)R;
   const float* un = static_cast<const float*>(a.u_n);
   const int32_t* nrow = gr.nrow[gi];
-  const float2* coef = gr.coef2[gi];
   const float* craw = gr.coef[gi];
   for (int c = l8 * 4; c < R; c += 64) {
     const float* own = un + (size_t)row0 * rs + c;
     const float4 uo0 = __ldg(reinterpret_cast<const float4*>(own));
     const float4 uo1 = __ldg(reinterpret_cast<const float4*>(own + 32));
     float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
-#pragma unroll UNROLL
+#pragma unroll 1
     for (int e = p0; e < p1; ++e) {
       const float* nb = un + (size_t)__ldg(nrow + e) * rs + c;
       const float4 g0 = __ldg(reinterpret_cast<const float4*>(nb));
       const float4 g1 = __ldg(reinterpret_cast<const float4*>(nb + 32));
-      float2 cv;
-      if (RAW) { const float cr = __ldg(craw + e); cv = make_float2(cr, cr); }
-      else cv = __ldg(coef + e);
+      const float cr = __ldg(craw + e);
+      const float2 cv = make_float2(cr, cr);
       acc0 = f4fma(cv, f4sub(uo0, g0), acc0);
       acc1 = f4fma(cv, f4sub(uo1, g1), acc1);
     }
@@ -135,7 +121,7 @@ __device__ __forceinline__ void group4_fluid(const StepArgs& a, const GroupArgs&
   }
 }
 
-template <int BS, int UNROLL, bool LATE_UP, bool RAW, int LPN>
+template <int BS, int LPN>
 __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& gr, int gi, int node,
                                             int l16) {
   const int4 rec = __ldg(gr.rec[gi] + node);
@@ -144,35 +130,28 @@ __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& 
   const size_t rs = (size_t)R;
   const float* un = static_cast<const float*>(a.u_n);
   const int32_t* nrow = gr.nrow[gi];
-  const float2* coef = gr.coef2[gi];
   const float* craw = gr.coef[gi];
   for (int c = l16 * 4; c < R; c += 4 * LPN) {
     float4 uo[BS], up[BS], acc[BS];
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
       uo[k] = __ldg(reinterpret_cast<const float4*>(un + (size_t)(row0 + k) * rs + c));
-      if (!LATE_UP)
-        up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) +
-                                                        (size_t)(row0 + k) * rs + c));
+      up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) +
+                                                      (size_t)(row0 + k) * rs + c));
       acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-#pragma unroll UNROLL
+#pragma unroll (BS == 1 ? 2 : 1)
     for (int e = p0; e < p1; ++e)
-      group4_nbr<BS, RAW>(un + (size_t)__ldg(nrow + e) * rs + c, coef, craw, e, rs, uo, acc);
+      group4_nbr<BS>(un + (size_t)__ldg(nrow + e) * rs + c, craw, e, rs, uo, acc);
 #pragma unroll
-    for (int k = 0; k < BS; ++k) {
-      const int row = row0 + k;
-      if (LATE_UP)
-        up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) + (size_t)row * rs + c));
-      finish4(a, row, c, uo[k], acc[k], up[k]);
-    }
+    for (int k = 0; k < BS; ++k) finish4(a, row0 + k, c, uo[k], acc[k], up[k]);
   }
 }
 
 // 128 threads = 128 / LPN nodes of LPN lanes each (LPN = 16 for R a
 // multiple of 64, 8 for R = 32, 4 for R = 16); gr.blk_begin must hold the
 // CTA ranges for 128 / LPN nodes per CTA.
-template <int UNROLL, int MINB, bool LATE_UP, bool RAW, int LPN = 16>
+template <int MINB, int LPN = 16>
 __global__ void __launch_bounds__(128, MINB) step_f32_group4(StepArgs a, GroupArgs gr) {
   const int b = blockIdx.x;
   int gi = 0;
@@ -182,16 +161,17 @@ __global__ void __launch_bounds__(128, MINB) step_f32_group4(StepArgs a, GroupAr
   if (LPN == 16 && gr.bs[gi] == 1) {                    // one-DOF nodes: 8 lanes, 16 nodes per CTA
     const int node = (b - gr.blk_begin[gi]) * 16 + (threadIdx.x >> 3);
     if (node >= gr.n_nodes[gi]) return;
-    group4_fluid<UNROLL, RAW>(a, gr, gi, node, threadIdx.x & 7);
+    group4_fluid(a, gr, gi, node, threadIdx.x & 7);
     return;
   }
   const int node = (b - gr.blk_begin[gi]) * (128 / LPN) + threadIdx.x / LPN;
   if (node >= gr.n_nodes[gi]) return;
-  if (gr.bs[gi] == 1) group4_node<1, UNROLL * 2, LATE_UP, RAW, LPN>(a, gr, gi, node, threadIdx.x % LPN);
-  else group4_node<2, UNROLL, LATE_UP, RAW, LPN>(a, gr, gi, node, threadIdx.x % LPN);
+  if (gr.bs[gi] == 1) group4_node<1, LPN>(a, gr, gi, node, threadIdx.x % LPN);
+  else group4_node<2, LPN>(a, gr, gi, node, threadIdx.x % LPN);
 }
 
-// The variants of the half-warp family for lanes-per-node LPN.
+// The variants of the half-warp family for lanes-per-node LPN: 20 at 12 CTAs
+// per SM, 22 at 10.
 template <int LPN>
 static void launch_group4(const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {
   GroupArgs g = gr;
@@ -202,15 +182,8 @@ static void launch_group4(const StepArgs& a, const GroupArgs& gr, int variant, c
     blocks += (g.n_nodes[k] + npc - 1) / npc;
   }
   g.blk_begin[g.n_groups] = blocks;
-  switch (variant) {
-    case 16: step_f32_group4<1, 10, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 17: step_f32_group4<2, 8, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 18: step_f32_group4<1, 12, false, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 19: step_f32_group4<1, 12, true, false, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 20: step_f32_group4<1, 12, false, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    case 21: step_f32_group4<1, 12, true, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-    default: step_f32_group4<1, 10, false, true, LPN><<<blocks, 128, 0, st>>>(a, g); break;
-  }
+  if (variant == 22) step_f32_group4<10, LPN><<<blocks, 128, 0, st>>>(a, g);
+  else step_f32_group4<12, LPN><<<blocks, 128, 0, st>>>(a, g);
 }
 
 cudaError_t launch_group4_variant(int lpn, const StepArgs& a, const GroupArgs& gr, int variant, cudaStream_t st) {

@@ -159,42 +159,19 @@ struct bfe_plan {
   bfe_stats last{};
   // autotuned batched-kernel variant per R (chosen on the first run with that R)
   std::map<int64_t, int> variant_of_R;
-  // node-block operator (FP32 difference form with node information)
-  bool have_node_blocks = false;
-  int32_t n_nodes = 0, max_nbr = 0, max_coef = 0;
-  bfe_host::DevBuf<uint32_t> node_word;
-  bfe_host::DevBuf<int32_t> nbr_ptr, coef_ptr;
-  bfe_host::DevBuf<uint32_t> gword;
-  bfe_host::DevBuf<float> coef;
+  int32_t n_nodes = 0;              // nodes given by dof_node / dof_type
   // group block-sparse operator (FP32 difference form)
   bool have_groups = false;
   bfe::GroupArgs groups{};
   bfe_host::DevBuf<int32_t> g_row0[bfe::kMaxGroups], g_nptr[bfe::kMaxGroups], g_nrow[bfe::kMaxGroups];
-  bfe_host::DevBuf<int32_t> g_frow[bfe::kMaxGroups];
   bfe_host::DevBuf<float2> g_coef2[bfe::kMaxGroups];
   bfe_host::DevBuf<int4> g_rec[bfe::kMaxGroups];
-  bfe_host::DevBuf<int32_t> g_cofs[bfe::kMaxGroups];
-  bfe_host::DevBuf<float2> g_coefp[bfe::kMaxGroups];
-  bfe_host::DevBuf<int> d_err;
-  bfe::TmaArgs tma{};
   bfe_host::DevBuf<float> g_coef[bfe::kMaxGroups];
   bfe_host::DevBuf<double> g_coef64[bfe::kMaxGroups];
   // BFE_MODE_V5: K, C (FP64 CSR) and the lumped mass, for the
   // prescribed-displacement rows of bfe_run_v5
   bfe_host::Csr hK, hC;
   std::vector<double> h_m;
-  bfe::NodeArgs node_args() const {
-    bfe::NodeArgs g{};
-    g.n_nodes = n_nodes;
-    g.node_word = node_word.p;
-    g.nbr_ptr = nbr_ptr.p;
-    g.gword = gword.p;
-    g.coef_ptr = coef_ptr.p;
-    g.coef = coef.p;
-    g.max_nbr = max_nbr;
-    g.max_coef = max_coef;
-    return g;
-  }
 };
 
 namespace bfe_host {

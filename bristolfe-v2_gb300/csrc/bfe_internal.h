@@ -93,25 +93,6 @@ __device__ __forceinline__ int64_t step_index(const StepArgs& a) {
   return a.ti_dev ? *a.ti_dev + a.ti : a.ti;
 }
 
-// Node-block operator (FP32 difference form): all DOF rows of one mesh node
-// are produced together from the neighbour DOF rows they couple to.
-//   node_word[a]  = base row of node a (bits 0-29) | (rows - 1) << 30
-//   nbr_ptr[a]    = first gathered row of node a (n_nodes + 1 entries)
-//   gword[e]      = gathered row (bits 0-27) | slot << 28, slot = position in
-//                   node a's block of the DOF with the gathered row's type
-//   coef_ptr[a]   = first coefficient of node a; coefficients are
-//                   [gathered row][own row]
-struct NodeArgs {
-  int32_t n_nodes;
-  const uint32_t* node_word;
-  const int32_t* nbr_ptr;
-  const uint32_t* gword;
-  const int32_t* coef_ptr;
-  const float* coef;
-  int32_t max_nbr;            // largest neighbour count of a node
-  int32_t max_coef;           // largest coefficient count of a node
-};
-
 // Group block-sparse operator (FP32 difference form). DOF types that K
 // couples form groups (2D solid {1,2}, fluid {4}, 3D solid {1,2,3}); every
 // node carrying a group holds its rows consecutively, so each group is a
@@ -127,31 +108,20 @@ struct GroupArgs {
   const int32_t* nptr[kMaxGroups];   // neighbour list of each node (n_nodes + 1)
   const int32_t* nrow[kMaxGroups];   // first row of each neighbour block
   const float* coef[kMaxGroups];     // BS*BS per neighbour block, [own k][neighbour l]
-  const int32_t* frow[kMaxGroups];   // flat neighbour rows: BS rows per neighbour block
   const float2* coef2[kMaxGroups];   // the coefficients as broadcast pairs {c, c}
   const int4* rec[kMaxGroups];       // per node {first row, first neighbour block, neighbour count, 0}
   const double* coef64[kMaxGroups];  // FP64 plans: B per block (own block included), [own k][l]
 };
 
-// Extra data of the TMA-staged group kernel (bfe_tma.cu): per node the
-// 16-byte-aligned offset (in float2 units) of its coefficient pairs inside a
-// padded copy of the coefficient array, and the device error flag a bounded
-// wait sets when it runs out.
-struct TmaArgs {
-  const int32_t* cofs[kMaxGroups];
-  const float2* coefp[kMaxGroups];
-  int* err;
-};
-
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.
 cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
-// Number of kernel variants the autotuner may choose from for (precision, R).
-int batched_variants(int precision, int R, bool have_nodes, bool have_groups);
-// Whether variant v applies to (precision, R) (the autotuner skips the others).
-bool batched_variant_supported(int precision, int R, int variant, bool have_nodes, bool have_groups);
-cudaError_t launch_step_batched(const StepArgs& a, const NodeArgs* g, const GroupArgs* gr,
-                                int precision, int max_slice_entries, int variant,
-                                cudaStream_t s);                                      // any R
+// Kernel variants a batched run of (precision, R) may use, the default
+// first; writes them to out (at most 8) and returns their number.
+int batched_candidates(int precision, int R, bool have_groups, int max_bs, int* out);
+// Largest node block size (DOFs per node) of a group operator.
+int group_max_bs(const GroupArgs& g);
+cudaError_t launch_step_batched(const StepArgs& a, const GroupArgs* gr, int precision, int max_slice_entries,
+                                int variant, cudaStream_t s);                         // any R
 size_t batched_smem_bytes(int precision, int max_slice_entries);
 cudaError_t set_batched_smem_limit(int precision, size_t smem);
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);
@@ -309,11 +279,5 @@ inline bool first_on_device(std::atomic<uint64_t>& done) {
   const uint64_t bit = 1ull << dev;
   return (done.fetch_or(bit) & bit) == 0;
 }
-
-size_t tma_smem_bytes();
-// tm_un / tm_up: CUtensorMap (2D FP32 [n][R], box 64 x 1) of u_n and u_{n-1}.
-cudaError_t launch_step_tma(const StepArgs& a, const GroupArgs& gr, const TmaArgs& t,
-                            const struct CUtensorMap_st* tm_un, const struct CUtensorMap_st* tm_up,
-                            cudaStream_t s);
 
 }  // namespace bfe

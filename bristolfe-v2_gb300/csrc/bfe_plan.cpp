@@ -359,13 +359,9 @@ namespace {
 int create_plan(Csr K, Csr C, Csr M, double dt, int32_t solver_mode, int32_t precision,
                 const int64_t* dof_node, const int32_t* dof_type, uint32_t flags, bfe_plan** out) {
   if (flags & ~(uint32_t)BFE_PLAN_ONE_SOURCE) return fail(BFE_ERR_ARG, "unknown plan flags 0x%x", flags);
-  // the node-block and group block-sparse forms serve only runs with many
-  // right-hand sides; a one-source plan skips building them
+  // the group block-sparse form serves only runs with many right-hand
+  // sides; a one-source plan skips building it
   const bool batched_forms = !(flags & BFE_PLAN_ONE_SOURCE);
-  // a forced node-block variant (BFE_VARIANT = 4 or 5, the variant sweeps and
-  // tests) needs the node-block form even where the group form exists
-  const char* forced_variant = getenv("BFE_VARIANT");
-  const bool node_form_forced = forced_variant && (atoi(forced_variant) == 4 || atoi(forced_variant) == 5);
   if (solver_mode != BFE_MODE_VEL_CURRENT && solver_mode != BFE_MODE_VEL_LAST_HALF &&
       solver_mode != BFE_MODE_V5)
     return fail(BFE_ERR_ARG, "unknown solver_mode %d", solver_mode);
@@ -751,113 +747,21 @@ int create_plan(Csr K, Csr C, Csr M, double dt, int32_t solver_mode, int32_t pre
           continue;
         }
         CUDA_TRY(pl->g_coef[gi].upload(coef));
-        // flat neighbour rows, broadcast pairs and the padded pair copy (each
-        // node's pairs start on a 16-byte boundary), filled on threads
+        // the coefficients as broadcast pairs {c, c}, filled on threads
         const int64_t n_nodes_g = (int64_t)nodes.size();
-        std::vector<int32_t> frow(nrow.size() * bs);
         std::vector<float2> coef2(coef.size());
-        std::vector<int32_t> cofs(n_nodes_g);
-        size_t n_pairs = 0;
-        for (int64_t a0 = 0; a0 < n_nodes_g; ++a0) {
-          n_pairs += n_pairs & 1;
-          cofs[a0] = (int32_t)n_pairs;
-          n_pairs += (size_t)(nptr[a0 + 1] - nptr[a0]) * bs * bs;
-        }
-        n_pairs += n_pairs & 1;
-        if (n_pairs >= (size_t)INT32_MAX) return fail(BFE_ERR_UNSUPPORTED, "group operator too large");
-        std::vector<float2> coefp(std::max<size_t>(n_pairs, 1), make_float2(0.f, 0.f));
         const int n_fill = plan_threads(n_nodes_g, 4096);
         if (!parallel_chunks(n_nodes_g, n_fill, [&](int, int64_t q0, int64_t q1) {
-              for (int64_t a0 = q0; a0 < q1; ++a0) {
-                for (int32_t b = nptr[a0]; b < nptr[a0 + 1]; ++b)
-                  for (int l = 0; l < bs; ++l) frow[(size_t)b * bs + l] = nrow[b] + l;
-                const size_t c0 = (size_t)nptr[a0] * bs * bs, c1 = (size_t)nptr[a0 + 1] * bs * bs;
-                for (size_t k = c0; k < c1; ++k) {
-                  coef2[k] = make_float2(coef[k], coef[k]);
-                  coefp[cofs[a0] + (k - c0)] = coef2[k];
-                }
-              }
+              const size_t c0 = (size_t)nptr[q0] * bs * bs, c1 = (size_t)nptr[q1] * bs * bs;
+              for (size_t k = c0; k < c1; ++k) coef2[k] = make_float2(coef[k], coef[k]);
             }))
           return fail(BFE_ERR_OOM, "host allocation failed while building the group operator");
-        CUDA_TRY(pl->g_frow[gi].upload(frow));
-        pl->groups.frow[gi] = pl->g_frow[gi].p;
         CUDA_TRY(pl->g_coef2[gi].upload(coef2));
         pl->groups.coef2[gi] = pl->g_coef2[gi].p;
-        CUDA_TRY(pl->g_cofs[gi].upload(cofs));
-        CUDA_TRY(pl->g_coefp[gi].upload(coefp));
-        pl->tma.cofs[gi] = pl->g_cofs[gi].p;
-        pl->tma.coefp[gi] = pl->g_coefp[gi].p;
         pl->groups.coef[gi] = pl->g_coef[gi].p;
       }
       pl->groups.blk_begin[pl->groups.n_groups] = blocks;
       pl->have_groups = ok && blocks > 0;
-      if (pl->have_groups && !f64) {
-        CUDA_TRY(pl->d_err.alloc(1));
-        pl->tma.err = pl->d_err.p;
-      }
-    }
-  }
-  // Node-block form of the FP32 operator (kernels step_f32_node, batched
-  // variants 4 and 5), the fallback when the group form cannot be built or
-  // when one of its variants is forced: every row must use the difference
-  // form, node blocks must hold at most 3 DOFs, and every non-zero coupling
-  // to a neighbour DOF type must exist in the own block.
-  if (batched_forms && precision == BFE_PREC_SINGLE && have_nodes && direct_rows == 0 &&
-      (!pl->have_groups || node_form_forced)) {
-    bool ok = true;
-    std::vector<uint32_t> hw, hg;
-    std::vector<int32_t> hnp(1, 0), hcp(1, 0);
-    std::vector<float> hc;
-    int32_t max_nbr = 0, max_coef = 0;
-    int64_t b = 0;
-    std::vector<int64_t> cols;
-    while (b < n && ok) {
-      const int64_t nb = blk_len[b];
-      if (nb > 3 || b > 0x3FFFFFFF) { ok = false; break; }
-      hw.push_back((uint32_t)b | ((uint32_t)(nb - 1) << 30));
-      // every neighbour DOF row any of the node's rows couples to
-      cols.clear();
-      for (int64_t i = b; i < b + nb; ++i)
-        for (int64_t e = K.ptr[i]; e < K.ptr[i + 1]; ++e)
-          if (dof_node[K.idx[e]] != dof_node[b]) cols.push_back(K.idx[e]);
-      std::sort(cols.begin(), cols.end());
-      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-      for (int64_t j : cols) {
-        int64_t slot = -1;
-        for (int64_t t = 0; t < nb; ++t)
-          if (dof_type[b + t] == dof_type[j]) slot = t;
-        bool any = false;
-        for (int64_t i = 0; i < nb; ++i) {
-          const int64_t row = b + i;
-          const int64_t* beg = K.idx.data() + K.ptr[row];
-          const int64_t* end = K.idx.data() + K.ptr[row + 1];
-          const int64_t* hit = std::lower_bound(beg, end, j);
-          const double v = (hit != end && *hit == j) ? lscale[row] * K.val[hit - K.idx.data()] : 0.0;
-          any = any || v != 0.0;
-          hc.push_back((float)v);
-        }
-        if (slot < 0) {
-          if (any) ok = false;      // coupling to a type the node lacks
-          slot = 0;
-        }
-        hg.push_back((uint32_t)j | ((uint32_t)slot << bfe::kSlotShift));
-      }
-      max_nbr = std::max<int32_t>(max_nbr, (int32_t)cols.size());
-      max_coef = std::max<int32_t>(max_coef, (int32_t)(cols.size() * nb));
-      hnp.push_back((int32_t)hg.size());
-      hcp.push_back((int32_t)hc.size());
-      b += nb;
-    }
-    if (ok && hc.size() < (size_t)INT32_MAX) {
-      pl->have_node_blocks = true;
-      pl->n_nodes = (int32_t)hw.size();
-      pl->max_nbr = max_nbr;
-      pl->max_coef = max_coef;
-      CUDA_TRY(pl->node_word.upload(hw));
-      CUDA_TRY(pl->nbr_ptr.upload(hnp));
-      CUDA_TRY(pl->coef_ptr.upload(hcp));
-      CUDA_TRY(pl->gword.upload(hg));
-      CUDA_TRY(pl->coef.upload(hc));
     }
   }
   pl->nnz_operator = stored;

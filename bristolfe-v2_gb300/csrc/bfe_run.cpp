@@ -4,44 +4,29 @@
 //
 // Reference being replaced: code/internal/fn_explicit_dynamic_solver_v6.m
 // (time loop :161-218) and fn_explicit_dynamic_solver_v5.m:60-188.
+#include <mutex>
+#include <tuple>
+
 #include "bfe_host.h"
 
 using namespace bfe_host;
 
-// Tensor maps of the state buffers for the TMA-staged batched variant.
 namespace {
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
-                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
-                                  CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_tiled() {
-  static const EncodeTiledFn fn = [] {            // initialised once, thread-safe
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess && q == cudaDriverEntryPointSuccess)
-      return reinterpret_cast<EncodeTiledFn>(p);
-    return EncodeTiledFn(nullptr);
-  }();
-  return fn;
-}
-
-// 2D FP32 tensor map of an [n][R] state buffer with a 64 x 1 box (one
-// 64-RHS row segment; gather4 fetches four of them).
-bool make_state_map(CUtensorMap* m, void* base, int64_t n, int64_t R) {
-  EncodeTiledFn fn = encode_tiled();
-  if (!fn || R % 64 != 0 || n >= (int64_t)1 << 31) return false;
-  if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
-  const cuuint64_t dims[2] = {(cuuint64_t)R, (cuuint64_t)n};
-  const cuuint64_t strides[1] = {(cuuint64_t)R * sizeof(float)};
-  const cuuint32_t box[2] = {64, 1};
-  const cuuint32_t estr[2] = {1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
+// Batched-kernel choices kept for the life of the process, so that a plan
+// over the same operator shape (a new plan per load step or per call, as
+// the MEX gateway makes) does not time the candidates again. The key is the
+// device, the operator's rows and stored entries, R, precision and node
+// block size.
+struct TuneKey {
+  int device, prec, max_bs;
+  int64_t n, nnz, R;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(device, prec, max_bs, n, nnz, R) < std::tie(o.device, o.prec, o.max_bs, o.n, o.nnz, o.R);
+  }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, int> g_tune_cache;
 
 // Wall-clock limit of one run (bfe_plan_set_time_limit). After each chunk of
 // steps has been queued, wait for the chunk before it (so one chunk stays
@@ -210,39 +195,41 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   const bool timing = pl->timing;
   TimeLimit limit;
   CUDA_TRY(limit.start(pl->time_limit_s));
-  // Autotuner: on the first batched run with this R, time every kernel
-  // variant on a few steps of the real operator (state still zero, so the
-  // results are discarded by the real march that follows) and keep the
-  // fastest. BFE_VARIANT=<k> forces variant k (for sweeps).
-  // tensor maps of the three state buffers for the TMA-staged kernel
-  alignas(64) CUtensorMap tmaps[3];
-  bool have_tmaps = false;
-  if (pl->have_groups && prec == BFE_PREC_SINGLE && R % 64 == 0) {
-    have_tmaps = make_state_map(&tmaps[0], U[0], n, R) && make_state_map(&tmaps[1], U[1], n, R) &&
-                 make_state_map(&tmaps[2], U[2], n, R);
-    CUDA_TRY(cudaMemsetAsync(pl->d_err.p, 0, sizeof(int), st));
-  }
-  auto launch_batched = [&](const bfe::NodeArgs* gpp, const bfe::GroupArgs* grpp, int v, int ib_n,
-                            int ib_prev) -> cudaError_t {
-    if (v == 15) {
-      if (!grpp || !have_tmaps) return cudaErrorNotSupported;
-      return bfe::launch_step_tma(a, *grpp, pl->tma, &tmaps[ib_n], &tmaps[ib_prev], st);
-    }
-    return bfe::launch_step_batched(a, gpp, grpp, prec, pl->max_slice_entries, v, st);
+  // Autotuner: on the first batched run with a given operator shape and R,
+  // time each candidate kernel (bfe::batched_candidates) on a few steps of
+  // the real operator - the state is still zero, and the march that follows
+  // starts from rest again - and keep the fastest. The default (first)
+  // candidate stays unless another is at least 3 % faster, so that near-ties
+  // do not flip between runs. The choice is kept in the plan and for the
+  // process (g_tune_cache). BFE_VARIANT=<k> forces variant k (sweeps).
+  auto launch_batched = [&](const bfe::GroupArgs* grpp, int v) -> cudaError_t {
+    return bfe::launch_step_batched(a, grpp, prec, pl->max_slice_entries, v, st);
   };
   int variant = 0;
-  const bfe::NodeArgs g = pl->node_args();
-  const bfe::NodeArgs* gp = pl->have_node_blocks ? &g : nullptr;
   const bfe::GroupArgs* grp = pl->have_groups ? &pl->groups : nullptr;
   if (R > 1) {
-    const int nv = bfe::batched_variants(prec, (int)R, pl->have_node_blocks, pl->have_groups);
+    int cand[8];
+    const int max_bs = grp ? bfe::group_max_bs(*grp) : 0;
+    const int nc = bfe::batched_candidates(prec, (int)R, pl->have_groups, max_bs, cand);
+    variant = cand[0];
+    const TuneKey key{pl->device, prec, max_bs, n, pl->nnz_operator, R};
     auto it = pl->variant_of_R.find(R);
     const char* force = getenv("BFE_VARIANT");
-    if (force && nv > 1) {
-      variant = std::max(0, std::min(nv - 1, atoi(force)));
+    bool cached = false;
+    if (!force && it == pl->variant_of_R.end()) {
+      std::lock_guard<std::mutex> lock(g_tune_mutex);
+      auto c = g_tune_cache.find(key);
+      if (c != g_tune_cache.end()) {
+        variant = c->second;
+        pl->variant_of_R[R] = variant;
+        cached = true;
+      }
+    }
+    if (force) {
+      variant = atoi(force);
     } else if (it != pl->variant_of_R.end()) {
       variant = it->second;
-    } else if (nv > 1 && rs.ti_start < rs.n_t) {
+    } else if (!cached && nc > 1 && rs.ti_start < rs.n_t) {
       a.ti = rs.ti_start;
       a.u_prev = U[0];
       a.u_n = U[1];
@@ -250,26 +237,27 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
       cudaEvent_t e0, e1;
       CUDA_TRY(cudaEventCreate(&e0));
       CUDA_TRY(cudaEventCreate(&e1));
-      float best = 1e30f;
-      for (int v = 0; v < nv; ++v) {
-        if (v == 15 && !have_tmaps) continue;
-        if (!bfe::batched_variant_supported(prec, (int)R, v, pl->have_node_blocks, pl->have_groups)) continue;
-        CUDA_TRY(launch_batched(gp, grp, v, 1, 0));   // warm
+      float t_default = 0.f, best = 1e30f;
+      for (int k = 0; k < nc; ++k) {
+        const int v = cand[k];
+        CUDA_TRY(launch_batched(grp, v));   // warm
         CUDA_TRY(cudaEventRecord(e0, st));
-        for (int k = 0; k < 3; ++k) CUDA_TRY(launch_batched(gp, grp, v, 1, 0));
+        for (int r = 0; r < 3; ++r) CUDA_TRY(launch_batched(grp, v));
         CUDA_TRY(cudaEventRecord(e1, st));
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;
         CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        stt.aux_launches += 4;
+        if (k == 0) t_default = ms;
         if (ms < best) { best = ms; variant = v; }
       }
+      if (best > 0.97f * t_default) variant = cand[0];
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * state_bytes, st));
-      if (rs.d_hist && rs.hist_idx.size()) {
-        // the tuning launches wrote zero history at ti_start; nothing to undo
-      }
       pl->variant_of_R[R] = variant;
+      std::lock_guard<std::mutex> lock(g_tune_mutex);
+      g_tune_cache[key] = variant;
     }
   }
   stt.variant = variant;
@@ -297,7 +285,7 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
     a.u_n = U[icur];
     a.u_new = U[inew];
     if (rec && timing) CUDA_TRY(mark(ev_step));
-    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st) : launch_batched(gp, grp, variant, icur, iprev);
+    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st) : launch_batched(grp, variant);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (rec && timing) CUDA_TRY(mark(ev_step));
     stt.step_launches++;
@@ -413,11 +401,6 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   CUDA_TRY(cudaStreamSynchronize(st));
   int nonfinite = 0;
   CUDA_TRY(cudaMemcpy(&nonfinite, pl->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
-  if (have_tmaps) {
-    int err = 0;
-    CUDA_TRY(cudaMemcpy(&err, pl->d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) return fail(BFE_ERR_CUDA, "a TMA stage wait exceeded its iteration limit");
-  }
   for (size_t k = 0; k + 1 < ev_step.size(); k += 2) {
     float ms = 0;
     CUDA_TRY(cudaEventElapsedTime(&ms, ev_step[k], ev_step[k + 1]));
