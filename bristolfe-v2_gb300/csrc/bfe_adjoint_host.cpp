@@ -120,41 +120,55 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   const int rk = bfe::grad_factor_rank(ndf);
   bool factored = false;
   if (rk > 0) {
-    std::vector<double> W((size_t)n_el * ndf * rk);
+    // traversal order: a stable counting sort by the lowest DOF row
+    std::vector<int32_t> ord(n_el);
+    {
+      std::vector<int64_t> key(n_el), start(n + 2, 0);
+      for (int64_t e = 0; e < n_el; ++e) {
+        int64_t k = n;                                   // elements without DOFs last
+        for (int i = 0; i < ndf; ++i)
+          if (el_dof[e * ndf + i] >= 0) k = std::min<int64_t>(k, el_dof[e * ndf + i]);
+        key[e] = k;
+        ++start[k + 1];
+      }
+      for (int64_t k = 0; k <= n; ++k) start[k + 1] += start[k];
+      for (int64_t e = 0; e < n_el; ++e) ord[start[key[e]]++] = (int32_t)e;
+    }
+    // factors in traversal order, written in the plan precision on the host
+    // threads straight into the upload buffer
+    std::vector<unsigned char> wbuf((size_t)n_el * ndf * rk * es);
+    std::vector<int32_t> dof_w((size_t)n_el * ndf);
     std::atomic<bool> ok{true};
     const int nth = plan_threads(n_el, 8192);
-    const bool done = parallel_chunks(n_el, nth, [&](int, int64_t b, int64_t e_end) {
-      std::vector<double> A((size_t)ndf * ndf);
-      for (int64_t e = b; e < e_end && ok; ++e) {
-        for (int i = 0; i < ndf; ++i)
+    const bool done = parallel_chunks(n_el, nth, [&](int, int64_t k0, int64_t k1) {
+      std::vector<double> A((size_t)ndf * ndf), W((size_t)ndf * rk);
+      for (int64_t k = k0; k < k1 && ok; ++k) {
+        const int64_t e = ord[k];
+        for (int i = 0; i < ndf; ++i) {
+          dof_w[k * ndf + i] = (int32_t)el_dof[e * ndf + i];
           for (int j = 0; j < ndf; ++j) {
             const bool use = el_dof[e * ndf + i] >= 0 && el_dof[e * ndf + j] >= 0;
             A[i * ndf + j] = use ? ke[(e * ndf + i) * ndf + j] : 0.0;
           }
-        if (factor_psd(A.data(), ndf, rk, W.data() + (size_t)e * ndf * rk) < 0) ok = false;
+        }
+        if (factor_psd(A.data(), ndf, rk, W.data()) < 0) {
+          ok = false;
+          break;
+        }
+        unsigned char* dst = wbuf.data() + (size_t)k * ndf * rk * es;
+        for (int i = 0; i < ndf * rk; ++i) {
+          if (prec == BFE_PREC_DOUBLE) std::memcpy(dst + i * es, &W[i], es);
+          else {
+            const float f = (float)W[i];
+            std::memcpy(dst + i * es, &f, es);
+          }
+        }
       }
     });
     if (done && ok) {
-      std::vector<int64_t> key(n_el);
-      for (int64_t e = 0; e < n_el; ++e) {
-        int64_t k = INT64_MAX;
-        for (int i = 0; i < ndf; ++i)
-          if (el_dof[e * ndf + i] >= 0) k = std::min<int64_t>(k, el_dof[e * ndf + i]);
-        key[e] = k;
-      }
-      std::vector<int32_t> ord(n_el);
-      std::iota(ord.begin(), ord.end(), 0);
-      std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
-      std::vector<int32_t> dof_w((size_t)n_el * ndf);
-      std::vector<double> w_sorted((size_t)n_el * ndf * rk);
-      for (int64_t k = 0; k < n_el; ++k) {
-        const int64_t e = ord[k];
-        for (int i = 0; i < ndf; ++i) dof_w[k * ndf + i] = (int32_t)el_dof[e * ndf + i];
-        std::copy(W.begin() + e * ndf * rk, W.begin() + (e + 1) * ndf * rk, w_sorted.begin() + k * ndf * rk);
-      }
       CUDA_TRY(d_dof_w.upload(dof_w));
       CUDA_TRY(d_out.upload(ord));
-      CUDA_TRY(d_w.upload(cast_bytes(prec, w_sorted.data(), n_el * ndf * rk)));
+      CUDA_TRY(d_w.upload(wbuf));
       factored = true;
     }
   }
