@@ -150,7 +150,7 @@ KERNEL_NAMES = {
     0: "step_batched<float,2> (slice-staged rows)",
     9: "step_f32_group2<2,1,1>", 10: "step_f32_group2<2,2,1>", 11: "step_f32_group2<2,4,1>",
     12: "step_f32_group2<2,1,4>", 13: "step_f32_group2<2,1,6>", 14: "step_f32_group2<2,1,8>",
-    20: "step_f32_group4<12>", 22: "step_f32_group4<10>", 24: "step_f32_tile<6>", 25: "step_f32_tile<5>",
+    20: "step_f32_group4<12>", 22: "step_f32_group4<10>",
 }
 
 

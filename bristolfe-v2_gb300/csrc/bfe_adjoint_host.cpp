@@ -204,8 +204,7 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   }
   auto step = [&](bfe::StepArgs& a) -> int {
     cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, grp, prec, pl->max_slice_entries, variant, st,
-                                                      pl->have_tiles ? &pl->tiles : nullptr);
+                           : bfe::launch_step_batched(a, grp, prec, pl->max_slice_entries, variant, st);
     if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
     if (pl->n_int) {
       e = bfe::launch_interface_fixup(a, prec, st);

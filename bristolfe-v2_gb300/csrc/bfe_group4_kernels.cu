@@ -170,112 +170,6 @@ __global__ void __launch_bounds__(128, MINB) step_f32_group4(StepArgs a, GroupAr
   else group4_node<2, LPN>(a, gr, gi, node, threadIdx.x % LPN);
 }
 
-// Tile-staged form (R a multiple of 64, node blocks of at most 2 DOFs): a
-// CTA takes one tile - a compact patch of a group's nodes - and, for each
-// 64-RHS chunk, first stages every node block the tile touches (its own and
-// its neighbour blocks, listed when the plan was built) from u_n into shared
-// memory: one 256-byte row per 16 threads, all loads independent, so a CTA
-// keeps the whole neighbourhood in flight instead of one dependent gather
-// per neighbour. Then each node is computed as in step_f32_group4 (a
-// half-warp per two-DOF node, 8 lanes per one-DOF node) with the gathers
-// read from shared memory.
-__device__ __forceinline__ void tile_node2(const StepArgs& a, const GroupArgs& gr, const TileArgs& tl, int gi,
-                                           int j, int c, int q, const float4* s_u) {
-  const int node = __ldg(tl.node[gi] + j);
-  const int4 rec = __ldg(gr.rec[gi] + node);
-  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
-  const int os = __ldg(tl.oslot[gi] + node);
-  const float* craw = gr.coef[gi];
-  const int16_t* ns = tl.nslot[gi];
-  const size_t rs = (size_t)a.R;
-  float4 uo[2], up[2], acc[2];
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    uo[k] = s_u[(os * 2 + k) * 16 + q];
-    up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) + (size_t)(row0 + k) * rs +
-                                                    c + 4 * q));
-    acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  for (int e = p0; e < p1; ++e) {
-    const int sl = __ldg(ns + e);
-    const float4 cr = __ldg(reinterpret_cast<const float4*>(craw + (size_t)e * 4));
-    const float4 g0 = s_u[sl * 32 + q], g1 = s_u[sl * 32 + 16 + q];
-    const float4 d0 = f4sub(uo[0], g0), d1 = f4sub(uo[1], g1);
-    acc[0] = f4fma(make_float2(cr.x, cr.x), d0, acc[0]);
-    acc[0] = f4fma(make_float2(cr.y, cr.y), d1, acc[0]);
-    acc[1] = f4fma(make_float2(cr.z, cr.z), d0, acc[1]);
-    acc[1] = f4fma(make_float2(cr.w, cr.w), d1, acc[1]);
-  }
-#pragma unroll
-  for (int k = 0; k < 2; ++k) finish4(a, row0 + k, c + 4 * q, uo[k], acc[k], up[k]);
-}
-
-__device__ __forceinline__ void tile_node1(const StepArgs& a, const GroupArgs& gr, const TileArgs& tl, int gi,
-                                           int j, int c, int l8, const float4* s_u) {
-  const int node = __ldg(tl.node[gi] + j);
-  const int4 rec = __ldg(gr.rec[gi] + node);
-  const int row0 = rec.x, p0 = rec.y, p1 = rec.y + rec.z;
-  const int os = __ldg(tl.oslot[gi] + node);
-  const float* craw = gr.coef[gi];
-  const int16_t* ns = tl.nslot[gi];
-  const float4 uo0 = s_u[os * 16 + l8], uo1 = s_u[os * 16 + 8 + l8];
-  float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
-  for (int e = p0; e < p1; ++e) {
-    const int sl = __ldg(ns + e);
-    const float cr = __ldg(craw + e);
-    const float2 cv = make_float2(cr, cr);
-    acc0 = f4fma(cv, f4sub(uo0, s_u[sl * 16 + l8]), acc0);
-    acc1 = f4fma(cv, f4sub(uo1, s_u[sl * 16 + 8 + l8]), acc1);
-  }
-  const float* upv = static_cast<const float*>(a.u_prev) + (size_t)row0 * a.R + c + 4 * l8;
-  finish4(a, row0, c + 4 * l8, uo0, acc0, __ldcs(reinterpret_cast<const float4*>(upv)));
-  finish4(a, row0, c + 32 + 4 * l8, uo1, acc1, __ldcs(reinterpret_cast<const float4*>(upv + 32)));
-}
-
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) step_f32_tile(StepArgs a, GroupArgs gr, TileArgs tl) {
-  extern __shared__ float4 s_u[];
-  const int b = blockIdx.x;
-  int gi = 0;
-#pragma unroll
-  for (int k = 1; k < kMaxGroups; ++k)
-    if (k < gr.n_groups && b >= tl.tile_begin[k]) gi = k;
-  const int t = b - tl.tile_begin[gi];
-  const int bs = gr.bs[gi];
-  const int kb0 = __ldg(tl.blk_ptr[gi] + t), nb = __ldg(tl.blk_ptr[gi] + t + 1) - kb0;
-  const int nd0 = __ldg(tl.node_ptr[gi] + t), nn = __ldg(tl.node_ptr[gi] + t + 1) - nd0;
-  const float* un = static_cast<const float*>(a.u_n);
-  const int32_t* brow = tl.blk_row[gi] + kb0;
-  const size_t rs = (size_t)a.R;
-  const int per = bs * 16;                                   // float4 per staged block
-  for (int c = 0; c < a.R; c += 64) {
-    if (c) __syncthreads();                                  // the previous chunk is consumed
-    for (int k = threadIdx.x; k < nb * per; k += blockDim.x) {
-      const int blk = k / per, rem = k - blk * per;
-      const int row = __ldg(brow + blk) + (rem >> 4);
-      s_u[k] = __ldg(reinterpret_cast<const float4*>(un + (size_t)row * rs + c) + (rem & 15));
-    }
-    __syncthreads();
-    if (bs == 2) {
-      for (int j = threadIdx.x >> 4; j < nn; j += blockDim.x >> 4)
-        tile_node2(a, gr, tl, gi, nd0 + j, c, threadIdx.x & 15, s_u);
-    } else {
-      for (int j = threadIdx.x >> 3; j < nn; j += blockDim.x >> 3)
-        tile_node1(a, gr, tl, gi, nd0 + j, c, threadIdx.x & 7, s_u);
-    }
-  }
-}
-
-cudaError_t launch_tile_variant(const StepArgs& a, const GroupArgs& gr, const TileArgs& tl, int variant,
-                                cudaStream_t st) {
-  const int blocks = tl.tile_begin[gr.n_groups];
-  const size_t smem = (size_t)tl.max_rows * 256;
-  if (blocks < 1) return cudaSuccess;
-  if (variant == 25) step_f32_tile<5><<<blocks, 256, smem, st>>>(a, gr, tl);
-  else step_f32_tile<6><<<blocks, 256, smem, st>>>(a, gr, tl);
-  return cudaGetLastError();
-}
-
 // The variants of the half-warp family for lanes-per-node LPN: 20 at 12 CTAs
 // per SM, 22 at 10.
 template <int LPN>

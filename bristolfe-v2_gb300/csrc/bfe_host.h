@@ -168,12 +168,6 @@ struct bfe_plan {
   bfe_host::DevBuf<int4> g_rec[bfe::kMaxGroups];
   bfe_host::DevBuf<float> g_coef[bfe::kMaxGroups];
   bfe_host::DevBuf<double> g_coef64[bfe::kMaxGroups];
-  // tiles of the tile-staged FP32 kernel (bfe::TileArgs)
-  bool have_tiles = false;
-  bfe::TileArgs tiles{};
-  bfe_host::DevBuf<int32_t> t_blk_ptr[bfe::kMaxGroups], t_blk_row[bfe::kMaxGroups], t_node_ptr[bfe::kMaxGroups],
-      t_node[bfe::kMaxGroups], t_oslot[bfe::kMaxGroups];
-  bfe_host::DevBuf<int16_t> t_nslot[bfe::kMaxGroups];
   // BFE_MODE_V5: K, C (FP64 CSR) and the lumped mass, for the
   // prescribed-displacement rows of bfe_run_v5
   bfe_host::Csr hK, hC;

@@ -113,39 +113,15 @@ struct GroupArgs {
   const double* coef64[kMaxGroups];  // FP64 plans: B per block (own block included), [own k][l]
 };
 
-// Tiles of the tile-staged FP32 group kernel (step_f32_tile): compact
-// patches of a group's nodes, grown on the node graph when the plan is built.
-// A CTA stages every node block its tile touches (the tile's own blocks and
-// their neighbour blocks) from u_n into shared memory with independent
-// coalesced loads, then computes the tile's nodes from there. CTAs
-// [tile_begin[g], tile_begin[g+1]) take group g's tiles.
-struct TileArgs {
-  int32_t tile_begin[kMaxGroups + 1];
-  int32_t max_rows;                   // most state rows a tile stages (shared memory: 256 B each)
-  const int32_t* blk_ptr[kMaxGroups];  // staged blocks of each tile (n_tiles + 1)
-  const int32_t* blk_row[kMaxGroups];  // first row of each staged block
-  const int32_t* node_ptr[kMaxGroups]; // nodes of each tile (n_tiles + 1)
-  const int32_t* node[kMaxGroups];     // the group's node index of each tile node
-  const int32_t* oslot[kMaxGroups];    // per group node: the slot of its own block in its tile
-  const int16_t* nslot[kMaxGroups];    // per neighbour block entry: its slot in the node's tile
-};
-// Largest tile (nodes) and most staged blocks per tile the plan builds for
-// 2-DOF node blocks (twice both for 1-DOF blocks, the same shared memory).
-constexpr int kTileNodes = 32;
-constexpr int kTileBlocks = 64;
-
 // Kernel launchers (bfe_kernels.cu). Return cudaError_t of the launch.
 cudaError_t launch_step(const StepArgs& a, int precision, cudaStream_t s);           // R == 1
 // Kernel variants a batched run of (precision, R) may use, the default
 // first; writes them to out (at most 8) and returns their number.
-int batched_candidates(int precision, int R, bool have_groups, int max_bs, int* out, bool have_tiles = false);
+int batched_candidates(int precision, int R, bool have_groups, int max_bs, int* out);
 // Largest node block size (DOFs per node) of a group operator.
 int group_max_bs(const GroupArgs& g);
 cudaError_t launch_step_batched(const StepArgs& a, const GroupArgs* gr, int precision, int max_slice_entries,
-                                int variant, cudaStream_t s, const TileArgs* tl = nullptr);   // any R
-// The tile-staged kernel (bfe_group4_kernels.cu), variants 24 and 25.
-cudaError_t launch_tile_variant(const StepArgs& a, const GroupArgs& gr, const TileArgs& tl, int variant,
-                                cudaStream_t s);
+                                int variant, cudaStream_t s);                         // any R
 size_t batched_smem_bytes(int precision, int max_slice_entries);
 cudaError_t set_batched_smem_limit(int precision, size_t smem);
 cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_t s);

@@ -342,12 +342,9 @@ size_t batched_smem_bytes(int precision, int max_slice_entries) {
 //   9 - 14   packed warp-per-node kernel step_f32_group2 (unroll 1, 2, 4;
 //            occupancy hints 4, 6, 8 CTAs): 3-DOF node blocks (3D), R a
 //            multiple of 64
-//   24, 25   tile-staged kernel step_f32_tile at 6 or 5 CTAs of 256 threads
-//            per SM: plans with tiles (node blocks of at most 2 DOFs), R a
-//            multiple of 64
 // The first candidate is the default; the autotuner keeps it unless another
 // is clearly faster on the live operator.
-int batched_candidates(int precision, int R, bool have_groups, int max_bs, int* out, bool have_tiles) {
+int batched_candidates(int precision, int R, bool have_groups, int max_bs, int* out) {
   int k = 0;
   if (precision == 0) {
     if (have_groups && R % 16 == 0) {
@@ -361,10 +358,6 @@ int batched_candidates(int precision, int R, bool have_groups, int max_bs, int* 
   if (have_groups && max_bs <= 2 && (R % 64 == 0 || R == 16 || R == 32)) {
     out[k++] = 20;
     out[k++] = 22;
-    if (have_tiles && R % 64 == 0) {
-      out[k++] = 24;
-      out[k++] = 25;
-    }
     return k;
   }
   if (have_groups && R % 64 == 0) {
@@ -382,7 +375,7 @@ int group_max_bs(const GroupArgs& g) {
 }
 
 cudaError_t launch_step_batched(const StepArgs& a, const GroupArgs* gr, int precision, int max_slice_entries,
-                                int variant, cudaStream_t st, const TileArgs* tl) {
+                                int variant, cudaStream_t st) {
   const int threads = 256;
   const size_t smem = batched_smem_bytes(precision, max_slice_entries);
   if (precision == 0) {
@@ -393,9 +386,7 @@ cudaError_t launch_step_batched(const StepArgs& a, const GroupArgs* gr, int prec
   const int maxbs = gr ? group_max_bs(*gr) : 0;
   const bool r64 = a.R % 64 == 0, r1632 = a.R == 16 || a.R == 32;
   const bool half_warp = variant == 20 || variant == 22;
-  if (gr && tl && (variant == 24 || variant == 25) && maxbs <= 2 && r64) {
-    return launch_tile_variant(a, *gr, *tl, variant, st);
-  } else if (gr && half_warp && maxbs <= 2 && (r64 || r1632)) {
+  if (gr && half_warp && maxbs <= 2 && (r64 || r1632)) {
     launch_group4_variant(r64 ? 16 : a.R == 32 ? 8 : 4, a, *gr, variant, st);
   } else if (gr && r64 && ((variant >= 9 && variant <= 14) || half_warp)) {
     // 3-DOF node blocks take the warp-per-node form

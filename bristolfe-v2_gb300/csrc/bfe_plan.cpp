@@ -354,92 +354,6 @@ int bfe_plan_create(const bfe_sparse* Kv, const bfe_sparse* Cv, const bfe_sparse
 
 namespace {
 
-// Tiles of one group for the tile-staged kernel (bfe::TileArgs). Patches are
-// grown greedily: from the lowest node not yet in a tile, add the free
-// neighbour with the most links into the patch (ties: the lowest index),
-// while the patch has fewer than max_nodes nodes and its own and neighbour
-// blocks fit max_blocks shared-memory slots. Seeds follow the node order, so
-// consecutive tiles are neighbours and share their halo blocks in L2.
-struct TileHost {
-  std::vector<int32_t> blk_ptr{0}, blk_row, node_ptr{0}, node, oslot;
-  std::vector<int16_t> nslot;
-  int max_blocks = 0;
-};
-
-bool build_tiles(const std::vector<int32_t>& row0, const std::vector<int32_t>& nptr,
-                 const std::vector<int32_t>& nrow, int max_nodes, int max_blocks, TileHost& th) {
-  const int32_t nn = (int32_t)row0.size();
-  std::vector<int32_t> nbr(nrow.size());
-  for (size_t e = 0; e < nrow.size(); ++e) {
-    auto it = std::lower_bound(row0.begin(), row0.end(), nrow[e]);
-    if (it == row0.end() || *it != nrow[e]) return false;      // a block outside the group
-    nbr[e] = (int32_t)(it - row0.begin());
-  }
-  th.oslot.assign(nn, -1);
-  th.nslot.assign(nrow.size(), -1);
-  std::vector<int32_t> tile_of(nn, -1), mark(nn, -1);
-  std::vector<int32_t> patch, blocks;
-  std::vector<std::pair<int32_t, int32_t>> cand;               // (free neighbour, links into the patch)
-  int32_t tile = 0;
-  for (int32_t seed = 0; seed < nn; ++seed) {
-    if (tile_of[seed] >= 0) continue;
-    patch.clear();
-    blocks.clear();
-    cand.clear();
-    // blocks a node would add to the tile (itself and its neighbours not yet staged)
-    auto new_blocks = [&](int32_t v) {
-      int k = mark[v] == tile ? 0 : 1;
-      for (int32_t e = nptr[v]; e < nptr[v + 1]; ++e) k += mark[nbr[e]] == tile ? 0 : 1;
-      return k;
-    };
-    auto add = [&](int32_t v) {
-      tile_of[v] = tile;
-      patch.push_back(v);
-      if (mark[v] != tile) { mark[v] = tile; blocks.push_back(v); }
-      for (int32_t e = nptr[v]; e < nptr[v + 1]; ++e) {
-        const int32_t w = nbr[e];
-        if (mark[w] != tile) { mark[w] = tile; blocks.push_back(w); }
-        if (tile_of[w] >= 0) continue;
-        bool found = false;
-        for (auto& c : cand)
-          if (c.first == w) { ++c.second; found = true; break; }
-        if (!found) cand.emplace_back(w, 1);
-      }
-    };
-    if ((int)(1 + nptr[seed + 1] - nptr[seed]) > max_blocks) return false;
-    add(seed);
-    while ((int)patch.size() < max_nodes) {
-      int best = -1;
-      for (size_t k = 0; k < cand.size(); ++k) {
-        const int32_t v = cand[k].first;
-        if (tile_of[v] >= 0) continue;
-        if (best < 0 || cand[k].second > cand[best].second ||
-            (cand[k].second == cand[best].second && v < cand[best].first))
-          best = (int)k;
-      }
-      if (best < 0) break;
-      const int32_t v = cand[best].first;
-      cand[best] = cand.back();                                  // taken or rejected
-      cand.pop_back();
-      if ((int)blocks.size() + new_blocks(v) > max_blocks) continue;
-      add(v);
-    }
-    std::sort(blocks.begin(), blocks.end());                    // slots in row order
-    for (int32_t v : patch) {
-      th.node.push_back(v);
-      th.oslot[v] = (int32_t)(std::lower_bound(blocks.begin(), blocks.end(), v) - blocks.begin());
-      for (int32_t e = nptr[v]; e < nptr[v + 1]; ++e)
-        th.nslot[e] = (int16_t)(std::lower_bound(blocks.begin(), blocks.end(), nbr[e]) - blocks.begin());
-    }
-    for (int32_t b : blocks) th.blk_row.push_back(row0[b]);
-    th.blk_ptr.push_back((int32_t)th.blk_row.size());
-    th.node_ptr.push_back((int32_t)th.node.size());
-    th.max_blocks = std::max(th.max_blocks, (int)blocks.size());
-    ++tile;
-  }
-  return true;
-}
-
 // Plan creation from owned CSR matrices (bfe_plan_create_ex converts its
 // views; bfe_plan_create_multi hands over the joined operator).
 int create_plan(Csr K, Csr C, Csr M, double dt, int32_t solver_mode, int32_t precision,
@@ -745,7 +659,6 @@ int create_plan(Csr K, Csr C, Csr M, double dt, int32_t solver_mode, int32_t pre
     }
     if (ok) {
       int32_t blocks = 0;
-      bool tiles_ok = !f64;
       pl->groups.n_groups = (int32_t)types.size();
       for (size_t gi = 0; gi < types.size() && ok; ++gi) {
         const int bs = (int)types[gi].size();
@@ -846,34 +759,9 @@ int create_plan(Csr K, Csr C, Csr M, double dt, int32_t solver_mode, int32_t pre
         CUDA_TRY(pl->g_coef2[gi].upload(coef2));
         pl->groups.coef2[gi] = pl->g_coef2[gi].p;
         pl->groups.coef[gi] = pl->g_coef[gi].p;
-        // tiles of the tile-staged kernel (node blocks of at most 2 DOFs)
-        if (bs <= 2 && tiles_ok) {
-          TileHost th;
-          tiles_ok = build_tiles(row0s[gi], nptr, nrow, bs == 1 ? 2 * bfe::kTileNodes : bfe::kTileNodes,
-                                 bs == 1 ? 2 * bfe::kTileBlocks : bfe::kTileBlocks, th);
-          if (tiles_ok) {
-            CUDA_TRY(pl->t_blk_ptr[gi].upload(th.blk_ptr));
-            CUDA_TRY(pl->t_blk_row[gi].upload(th.blk_row));
-            CUDA_TRY(pl->t_node_ptr[gi].upload(th.node_ptr));
-            CUDA_TRY(pl->t_node[gi].upload(th.node));
-            CUDA_TRY(pl->t_oslot[gi].upload(th.oslot));
-            CUDA_TRY(pl->t_nslot[gi].upload(th.nslot));
-            pl->tiles.blk_ptr[gi] = pl->t_blk_ptr[gi].p;
-            pl->tiles.blk_row[gi] = pl->t_blk_row[gi].p;
-            pl->tiles.node_ptr[gi] = pl->t_node_ptr[gi].p;
-            pl->tiles.node[gi] = pl->t_node[gi].p;
-            pl->tiles.oslot[gi] = pl->t_oslot[gi].p;
-            pl->tiles.nslot[gi] = pl->t_nslot[gi].p;
-            pl->tiles.tile_begin[gi + 1] = pl->tiles.tile_begin[gi] + (int32_t)(th.blk_ptr.size() - 1);
-            pl->tiles.max_rows = std::max(pl->tiles.max_rows, th.max_blocks * bs);
-          }
-        } else {
-          tiles_ok = false;
-        }
       }
       pl->groups.blk_begin[pl->groups.n_groups] = blocks;
       pl->have_groups = ok && blocks > 0;
-      pl->have_tiles = pl->have_groups && !f64 && tiles_ok;
     }
   }
   pl->nnz_operator = stored;

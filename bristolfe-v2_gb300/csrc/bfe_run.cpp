@@ -202,16 +202,15 @@ int execute(bfe_plan* pl, RunSpec& rs, cudaStream_t st) {
   // candidate stays unless another is at least 3 % faster, so that near-ties
   // do not flip between runs. The choice is kept in the plan and for the
   // process (g_tune_cache). BFE_VARIANT=<k> forces variant k (sweeps).
-  const bfe::TileArgs* tlp = pl->have_tiles ? &pl->tiles : nullptr;
   auto launch_batched = [&](const bfe::GroupArgs* grpp, int v) -> cudaError_t {
-    return bfe::launch_step_batched(a, grpp, prec, pl->max_slice_entries, v, st, tlp);
+    return bfe::launch_step_batched(a, grpp, prec, pl->max_slice_entries, v, st);
   };
   int variant = 0;
   const bfe::GroupArgs* grp = pl->have_groups ? &pl->groups : nullptr;
   if (R > 1) {
     int cand[8];
     const int max_bs = grp ? bfe::group_max_bs(*grp) : 0;
-    const int nc = bfe::batched_candidates(prec, (int)R, pl->have_groups, max_bs, cand, pl->have_tiles);
+    const int nc = bfe::batched_candidates(prec, (int)R, pl->have_groups, max_bs, cand);
     variant = cand[0];
     const TuneKey key{pl->device, prec, max_bs, n, pl->nnz_operator, R};
     auto it = pl->variant_of_R.find(R);

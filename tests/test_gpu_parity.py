@@ -173,12 +173,11 @@ def test_errors_through_the_abi(bfe, plate):
             plan.run(t, [1, 2], np.ones((3, 20)), [1])             # 3 rows for 2 DOFs
 
 
-@pytest.mark.parametrize("variant", [0, 9, 10, 11, 12, 13, 14, 20, 22, 24, 25])
+@pytest.mark.parametrize("variant", [0, 9, 10, 11, 12, 13, 14, 20, 22])
 def test_every_batched_fp32_kernel_variant(bfe, coupled, variant, monkeypatch):
     """Each batched FP32 kernel (forced through BFE_VARIANT) gives the same
     answers: 0 the slice-staged row kernel, 9-14 the packed warp-per-node
-    group kernel, 20 and 22 the half-warp float4 group kernel, 24 and 25 the
-    tile-staged kernel."""
+    group kernel, 20 and 22 the half-warp float4 group kernel."""
     m = coupled
     nt = 150
     t, s = modelgen.pulse(nt, m["dt"])
