@@ -68,7 +68,7 @@ def build(verbose=False, force=False):
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB] + objs + \
-            ["-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+            ["-lcufft", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
         run(cmd)
     return LIB
 

@@ -4,11 +4,18 @@
 //   bfe_disps_to_forces   code/fn_convert_disps_to_forces_v2.m:1-31
 //
 // fn_convolve multiplies FFTs of 2 n_t points and keeps the first n_t
-// samples, i.e. the circular convolution of length 2 n_t; the kernel here
-// evaluates that sum directly over the signal's non-zero support:
+// samples, i.e. the circular convolution of length 2 n_t. A short signal g
+// (the toneburst: a few hundred non-zero samples) is applied as that sum
+// directly over its non-zero support:
 //   h[t] = sum_{tau <= t} g[tau] f[t - tau]
 //        + sum_{tau > n_t + t} g[tau] f[2 n_t + t - tau]   (wrap, g longer than n_t)
+// A long one (a recorded boundary history in the sub-domain pipeline,
+// subdoms/fn_run_subdomain_model.m:98-112) takes fn_convolve's own route on
+// cuFFT: real-to-complex FFTs of 2 n_t points, the pointwise product, the
+// inverse FFT scaled by 1 / (2 n_t), the first n_t samples - O(n_t log n_t)
+// per signal instead of O(n_t * support).
 #include <cuda_runtime.h>
+#include <cufft.h>
 
 #include <cstdint>
 #include <map>
@@ -101,6 +108,73 @@ __global__ void forces_kernel(int64_t n, int64_t n_t, int64_t n_force, const int
   out[(size_t)t * n_force + fr] = acc + sc + sk;
 }
 
+// F[s][k] *= G[k] * scale for the n_sig spectra of nc bins.
+__global__ void spectrum_product_kernel(int64_t nc, int64_t n_sig, cufftDoubleComplex* __restrict__ F,
+                                        const cufftDoubleComplex* __restrict__ G, double scale) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t s = blockIdx.y;
+  if (k >= nc || s >= n_sig) return;
+  const cufftDoubleComplex a = F[s * nc + k], b = G[k];
+  F[s * nc + k] = make_cuDoubleComplex((a.x * b.x - a.y * b.y) * scale, (a.x * b.y + a.y * b.x) * scale);
+}
+
+// Supports longer than this many samples take the FFT route.
+constexpr int64_t kFftSupport = 256;
+
+struct FftPlan {
+  cufftHandle h = 0;
+  bool ok = false;
+  ~FftPlan() { if (ok) cufftDestroy(h); }
+};
+
+#define CUFFT_TRY(x)                                                                 \
+  do {                                                                               \
+    const cufftResult r_ = (x);                                                      \
+    if (r_ != CUFFT_SUCCESS) return ffail(BFE_ERR_CUDA, "cuFFT call failed: " #x);   \
+  } while (0)
+
+// fn_convolve.m:22-33 on cuFFT for n_sig signals of n_t samples (d_f,
+// column-major) and g (host, n_g samples, truncated to 2 n_t like
+// fft(g, 2 n_t)).
+int launch_convolve_fft(int64_t n_t, int64_t n_sig, const double* d_f, const double* h_g, int64_t n_g,
+                        double* d_h, cudaStream_t st) {
+  const int64_t L = 2 * n_t, nc = n_t + 1;
+  if (L > 0x7fffffffLL || n_sig > 0x7fffffffLL) return ffail(BFE_ERR_UNSUPPORTED, "signals too long for one FFT");
+  DVec<double> pad, gpad;
+  DVec<cufftDoubleComplex> F, G;
+  FTRY(pad.alloc((size_t)L * n_sig));
+  FTRY(gpad.alloc((size_t)L));
+  FTRY(F.alloc((size_t)nc * n_sig));
+  FTRY(G.alloc((size_t)nc));
+  FTRY(cudaMemsetAsync(pad.p, 0, (size_t)L * n_sig * sizeof(double), st));
+  FTRY(cudaMemcpy2DAsync(pad.p, L * sizeof(double), d_f, n_t * sizeof(double), n_t * sizeof(double), n_sig,
+                         cudaMemcpyDeviceToDevice, st));
+  FTRY(cudaMemsetAsync(gpad.p, 0, (size_t)L * sizeof(double), st));
+  const int64_t ng = n_g < L ? n_g : L;
+  if (ng > 0) FTRY(cudaMemcpyAsync(gpad.p, h_g, ng * sizeof(double), cudaMemcpyHostToDevice, st));
+  int len = (int)L;
+  FftPlan fwd, one, inv;
+  CUFFT_TRY(cufftPlanMany(&fwd.h, 1, &len, nullptr, 1, (int)L, nullptr, 1, (int)nc, CUFFT_D2Z, (int)n_sig));
+  fwd.ok = true;
+  CUFFT_TRY(cufftPlan1d(&one.h, len, CUFFT_D2Z, 1));
+  one.ok = true;
+  CUFFT_TRY(cufftPlanMany(&inv.h, 1, &len, nullptr, 1, (int)nc, nullptr, 1, (int)L, CUFFT_Z2D, (int)n_sig));
+  inv.ok = true;
+  CUFFT_TRY(cufftSetStream(fwd.h, st));
+  CUFFT_TRY(cufftSetStream(one.h, st));
+  CUFFT_TRY(cufftSetStream(inv.h, st));
+  CUFFT_TRY(cufftExecD2Z(fwd.h, pad.p, F.p));
+  CUFFT_TRY(cufftExecD2Z(one.h, gpad.p, G.p));
+  const dim3 grid((unsigned)((nc + 255) / 256), (unsigned)n_sig);
+  spectrum_product_kernel<<<grid, 256, 0, st>>>(nc, n_sig, F.p, G.p, 1.0 / (double)L);
+  FTRY(cudaGetLastError());
+  CUFFT_TRY(cufftExecZ2D(inv.h, F.p, pad.p));
+  FTRY(cudaMemcpy2DAsync(d_h, n_t * sizeof(double), pad.p, L * sizeof(double), n_t * sizeof(double), n_sig,
+                         cudaMemcpyDeviceToDevice, st));
+  FTRY(cudaStreamSynchronize(st));
+  return BFE_OK;
+}
+
 // Non-zero support [g0, g1) of g restricted to 2 n_t points.
 void support(const double* g, int64_t n_g, int64_t n_t, int64_t& g0, int64_t& g1) {
   const int64_t n = n_g < 2 * n_t ? n_g : 2 * n_t;
@@ -114,6 +188,7 @@ int launch_convolve(int64_t n_t, int64_t n_sig, const double* d_f, const double*
                     double* d_h, cudaStream_t st) {
   int64_t g0, g1;
   support(h_g, n_g, n_t, g0, g1);
+  if (g1 - g0 > kFftSupport && n_sig <= 65535) return launch_convolve_fft(n_t, n_sig, d_f, h_g, n_g, d_h, st);
   DVec<double> d_g;
   FTRY(d_g.upload(h_g, (size_t)(g1 > 0 ? g1 : 0), st));
   if (g1 <= g0) {

@@ -27,8 +27,10 @@ def bfe():
     return bfe_gb300
 
 
-@pytest.mark.parametrize("glen", [0.5, 1.0, 3.0])
+@pytest.mark.parametrize("glen", [0.3, 0.5, 1.0, 3.0])
 def test_convolve_matches_fft_convolution(bfe, glen):
+    """Supports of 190 samples (direct sum) and 330 to 1,400 (the cuFFT route,
+    g truncated to 2 n_t like fft(g, 2 n_t))."""
     rng = np.random.default_rng(3)
     n = 700
     f = rng.standard_normal((n, 6))
@@ -36,6 +38,20 @@ def test_convolve_matches_fft_convolution(bfe, glen):
     g[: 20] = 0.0                                  # leading zeros (support search)
     ref = np.column_stack([subdomain.convolve(f[:, k], g) for k in range(f.shape[1])])
     assert _err(bfe.fn_convolve_gb300(f, g), ref) <= 1e-12
+
+
+def test_convolve_with_a_recorded_history(bfe):
+    """The sub-domain pipeline convolves recorded boundary histories (support
+    = the whole record, subdoms/fn_run_subdomain_model.m:98-112): 16,384
+    samples, 48 signals, against the oracle's FFT convolution."""
+    rng = np.random.default_rng(11)
+    n = 16384
+    f = rng.standard_normal((n, 48))
+    g = np.cumsum(rng.standard_normal(n)) * np.hanning(n)
+    out = bfe.fn_convolve_gb300(f, g)
+    for k in (0, 17, 47):
+        ref = subdomain.convolve(f[:, k], g)
+        assert _err(out[:, k], ref) <= 1e-12
 
 
 def test_fmc_from_a_batched_run(bfe):
