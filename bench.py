@@ -737,8 +737,9 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20, n_t=4000):
     triangles): 16 sources x 16 receivers, 4,000 samples, observed A-scans
     from a seeded +-5 % stiffness perturbation (1 mm Gaussian bumps),
     gradient of the misfit w.r.t. per-element stiffness scale and density
-    (sqrt(N) checkpoints) in FP32 and FP64, FP64 central differences on
-    n_fd random elements of the sensitive region."""
+    (backward segments of sqrt(N) steps; forward states kept on the device
+    when they fit) in FP32 and FP64, FP64 central differences on n_fd random
+    elements of the sensitive region."""
     m = model.steel_plate_adjoint()
     ke, mh, ch, dof = m["element_data"]
     n = m["K"].shape[0]
@@ -753,7 +754,7 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20, n_t=4000):
         obs = p.run_batched(t, srcs, sig, rec)
     K0, C0, M0 = model.assemble_from_elements(ke, mh, ch, dof, n, None, rho_e)
     res = {"n_dof": n, "elements": int(len(dof)), "sources": len(srcs), "receivers": int(rec.size),
-           "samples": n_t, "checkpoints": int(np.ceil(np.sqrt(n_t)))}
+           "samples": n_t, "segment_steps": int(np.ceil(np.sqrt(n_t)))}
     grads = {}
     for prec in ("single", "double"):
         with bfe_gb300.Plan(K0, C0, M0, dt, bfe_gb300.VEL_CURRENT, prec, m["gl"]) as p:
@@ -762,8 +763,11 @@ def adjoint_section(torch, bfe_gb300, model, n_fd=20, n_t=4000):
             t0 = time.perf_counter()
             J, gs, gr = p.adjoint_gradient((ke, mh, ch, dof), t, srcs, sig, rec, obs)
             el = time.perf_counter() - t0
+            kept = p.stats()["adjoint_kept"]
         grads[prec] = (J, gs, gr)
-        res["fp32" if prec == "single" else "fp64"] = {"gradient_s": el, "misfit": J}
+        res["fp32" if prec == "single" else "fp64"] = {
+            "gradient_s": el, "misfit": J,
+            "forward_states": "kept on the device" if kept else "recomputed from checkpoints"}
     J64, gs64, gr64 = grads["double"]
     _, gs32, gr32 = grads["single"]
     res["fp32_vs_fp64_rel"] = {"stiffness": float(np.linalg.norm(gs32 - gs64) / np.linalg.norm(gs64)),

@@ -75,7 +75,8 @@ class BfeStats(ctypes.Structure):
     _fields_ = [("step_launches", I64), ("aux_launches", I64), ("step_ms", ctypes.c_double),
                 ("aux_ms", ctypes.c_double), ("n_dof", I64), ("nnz_stored", I64),
                 ("nnz_padded", I64), ("n_interface", I64), ("n_direct_rows", I64),
-                ("variant", I64), ("n_nodes", I64), ("n_groups", I64)]
+                ("variant", I64), ("n_nodes", I64), ("n_groups", I64), ("adjoint_segments", I64),
+                ("adjoint_kept", I64)]
 
 
 SIGNATURES = {

@@ -324,9 +324,12 @@ class Plan:
     def adjoint_gradient(self, element_data, time, forcing_indices_per_source, forcing_functions,
                          history_indices, observed, ckpt_every=0, return_history=False):
         """Misfit J and its gradients w.r.t. per-element stiffness scale and
-        density (adjoint with checkpointing). element_data = (ke, mh, ch, dof)
-        with dof 0-based global rows (n_el x ndf, -1 unused); indices 1-based;
-        observed (q, n_t, R). Returns (J, g_stiff, g_rho[, hist])."""
+        density (discrete adjoint). element_data = (ke, mh, ch, dof) with dof
+        0-based global rows (n_el x ndf, -1 unused); indices 1-based; observed
+        (q, n_t, R). ckpt_every = 0 keeps every forward state on the device
+        when they fit (else checkpoints every ceil(sqrt(steps))); c > 0
+        recomputes segments of c steps from checkpoints. Returns (J, g_stiff,
+        g_rho[, hist])."""
         ke, mh, ch, dof = element_data
         ke = np.ascontiguousarray(ke, np.float64)
         mh = np.ascontiguousarray(mh, np.float64)

@@ -234,6 +234,76 @@ __global__ void __launch_bounds__(256) grad_stiff_w(int64_t n_el, const int32_t*
   if (sub == 0) gs[__ldg(el_out + e)] -= scale * a;
 }
 
+// FP32 form of grad_stiff_w for R a multiple of 4: each lane covers four
+// sources (one 16-byte load per row), the multiply-adds run in pairs (FFMA2,
+// W_e broadcast to both halves), row offsets are 32-bit (n R < 2^31), and a
+// DOF that is unused (-1) reads row 0 unmasked: its row of W_e is zero (the
+// host zeroes the unused rows and columns of K_e before factoring), so it
+// adds nothing while every load of a step issues unconditionally.
+template <int NDF, int RK>
+__global__ void __launch_bounds__(256) grad_stiff_wf(int64_t n_el, const int32_t* __restrict__ el_dof,
+                                                     const float* __restrict__ w,
+                                                     const int32_t* __restrict__ el_out,
+                                                     const float* __restrict__ lam, const float* __restrict__ u,
+                                                     int64_t stride, int n_steps, int R, int tpe, double scale,
+                                                     double* __restrict__ gs) {
+  constexpr int VEC = 4, H = 2;                       // sources per lane, float2 halves
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t e = gt / tpe;
+  const int sub = (int)(gt % tpe);
+  if (e >= n_el) return;       // whole groups leave together: tpe divides 32 and the block size
+  const int lane = threadIdx.x & 31;
+  const unsigned mask = tpe == 32 ? 0xffffffffu : ((1u << tpe) - 1u) << (lane & ~(tpe - 1));
+  uint32_t off[NDF];
+  float W[NDF][RK];
+#pragma unroll
+  for (int i = 0; i < NDF; ++i) {
+    const int d = __ldg(el_dof + e * NDF + i);
+    off[i] = (uint32_t)(d >= 0 ? d : 0) * (uint32_t)R;
+#pragma unroll
+    for (int q = 0; q < RK; ++q) W[i][q] = __ldg(w + (e * NDF + i) * RK + q);
+  }
+  const int nv = R / VEC;
+  StepSum<float> acc;
+  for (int k = 0; k < n_steps; ++k) {
+    const float* L = lam + (size_t)k * stride;          // lam_t
+    const float* U1 = u + (size_t)(k + 1) * stride;     // u_{t-1}
+    for (int cv = sub; cv < nv; cv += tpe) {
+      const uint32_t r = (uint32_t)cv * VEC;
+      float2 y[RK][H], z[RK][H];
+#pragma unroll
+      for (int q = 0; q < RK; ++q)
+#pragma unroll
+        for (int h = 0; h < H; ++h) y[q][h] = z[q][h] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < NDF; ++j) {
+        const float4 a4 = __ldg(reinterpret_cast<const float4*>(U1 + off[j] + r));
+        const float4 l4 = __ldg(reinterpret_cast<const float4*>(L + off[j] + r));
+        const float2 a[H] = {make_float2(a4.x, a4.y), make_float2(a4.z, a4.w)};
+        const float2 l[H] = {make_float2(l4.x, l4.y), make_float2(l4.z, l4.w)};
+#pragma unroll
+        for (int q = 0; q < RK; ++q) {
+          const float2 wq = make_float2(W[j][q], W[j][q]);
+#pragma unroll
+          for (int h = 0; h < H; ++h) {
+            y[q][h] = __ffma2_rn(wq, a[h], y[q][h]);
+            z[q][h] = __ffma2_rn(wq, l[h], z[q][h]);
+          }
+        }
+      }
+      float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < RK; ++q)
+#pragma unroll
+        for (int h = 0; h < H; ++h) s2 = __ffma2_rn(y[q][h], z[q][h], s2);
+      acc.add(s2.x + s2.y);
+    }
+  }
+  double a = acc.value();
+  for (int off2 = tpe >> 1; off2 > 0; off2 >>= 1) a += __shfl_xor_sync(mask, a, off2);
+  if (sub == 0) gs[__ldg(el_out + e)] -= scale * a;
+}
+
 // dJ/drho, per DOF: mh and ch are constant in time, so the density term
 // needs only, per DOF d and summed over the steps and sources,
 //   pw[d] += lam_t[d] (u_t - 2 u_{t-1} + u_{t-2})[d]
@@ -334,6 +404,19 @@ cudaError_t launch_stiff(const GradArgs& g, cudaStream_t st) {
 // sums and loads in flight within the register budget of 24 warps per SM
 template <typename T, int NDF, int RK>
 cudaError_t launch_stiff_w(const GradArgs& g, cudaStream_t st) {
+  if (sizeof(T) == 4 && g.R % 4 == 0 && g.n * g.R < (int64_t)INT32_MAX) {
+    const int tpe = lanes_for(g.R, 4);
+    const int threads = 256;
+    const int64_t blocks = (g.n_el * tpe + threads - 1) / threads;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const float* w = static_cast<const float*>(g.w);
+    const float* l = static_cast<const float*>(g.lam);
+    const float* u = static_cast<const float*>(g.u);
+    const double scale = g.dt * g.dt;
+    grad_stiff_wf<NDF, RK><<<(unsigned)blocks, threads, 0, st>>>(g.n_el, g.el_dof_w, w, g.el_out, l, u, g.stride,
+                                                                 g.n_steps, g.R, tpe, scale, g.gs);
+    return cudaGetLastError();
+  }
   constexpr int VMAX = sizeof(T) == 4 ? 2 : 1;
   const int vec = g.R % VMAX == 0 ? VMAX : 1;
   const int tpe = lanes_for(g.R, vec);

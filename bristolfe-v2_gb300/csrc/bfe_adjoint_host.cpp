@@ -45,11 +45,12 @@ int factor_psd(double* A, int ndf, int rk, double* W) {
 
 extern "C" {
 
-// Adjoint gradient of an A-scan misfit with sqrt(N)-step checkpointing (see
-// include/bfe_gb300.h). Forward march with checkpoints of (u_{t-2}, u_{t-1})
-// every c steps and the monitored history; residuals and misfit on the host
-// in FP64; backward sweep over segments: recompute the segment's states from
-// its checkpoint into consecutive slots, step the adjoint (the same
+// Adjoint gradient of an A-scan misfit (see include/bfe_gb300.h). Forward
+// march keeping every state on the device when they fit, else checkpoints of
+// (u_{t-2}, u_{t-1}) every c steps, and the monitored history; residuals and
+// misfit on the host in FP64; backward sweep over segments of c steps: take
+// the segment's forward states from the kept ones or recompute them from its
+// checkpoint into consecutive slots, step the adjoint (the same
 // operator, driven by the residuals) backwards through the segment into
 // slots of its own, then contract the whole segment into the per-element
 // stiffness accumulators and per-DOF density sums with one launch pair
@@ -101,13 +102,109 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   const int64_t c = ckpt_every > 0 ? ckpt_every : (int64_t)std::ceil(std::sqrt((double)steps));
   const int64_t n_seg = (steps + c - 1) / c;
 
-  // element data on the device
+  // forward inputs
+  const int64_t n_sig = frc_rows * R;
+  DevBuf<double> d_sig, d_hist;
+  {
+    std::vector<double> h((size_t)n_t * n_sig);
+    for (int64_t r = 0; r < R; ++r)
+      for (int64_t ti = 0; ti < n_t; ++ti)
+        for (int64_t k = 0; k < frc_rows; ++k)
+          h[(size_t)ti * n_sig + k + frc_rows * r] = frcs[k + frc_rows * (ti + n_t * r)];
+    CUDA_TRY(d_sig.upload(h));
+  }
+  const size_t hist_n = (size_t)q * n_t * R;
+  CUDA_TRY(d_hist.alloc(hist_n));
+  CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
+  std::vector<int64_t> hidx(hist_idx, hist_idx + q);
+  RunArrays rf;
+  bfe::StepArgs af;
+  if ((rc = prepare_run(pl, frc, hidx, R, n_t, n_sig, d_sig.p, d_hist.p, st, rf, af))) return rc;
+  const bool use_groups = pl->have_groups && (prec == BFE_PREC_SINGLE ? (R % 64 == 0 || R == 16 || R == 32)
+                                                                       : R % 16 == 0);
+  const bfe::GroupArgs* grp = use_groups ? &pl->groups : nullptr;
+  // the variant the forward runs chose for this R, else the default candidate
+  int variant = 0;
+  if (R > 1) {
+    int cand[8];
+    bfe::batched_candidates(prec, (int)R, use_groups, grp ? bfe::group_max_bs(*grp) : 0, cand);
+    variant = cand[0];
+    auto it = pl->variant_of_R.find(R);
+    if (it != pl->variant_of_R.end()) variant = it->second;
+  }
+  auto step = [&](bfe::StepArgs& a) -> int {
+    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
+                           : bfe::launch_step_batched(a, grp, prec, pl->max_slice_entries, variant, st);
+    if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
+    if (pl->n_int) {
+      e = bfe::launch_interface_fixup(a, prec, st);
+      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "interface kernel launch failed: %s", cudaGetErrorString(e));
+    }
+    return BFE_OK;
+  };
+  const size_t sb = (size_t)n * R * es;
+  // With ckpt_every = 0, every forward state stays on the device when the
+  // steps + 2 states and the adjoint's c + 2 segment slots fit in 3/4 of the
+  // free memory: state u_t sits in slot t - ti0 + 2 of d_all (slots 0 and 1
+  // hold the zero initial states), and the backward sweep contracts straight
+  // from it instead of recomputing each segment from a checkpoint.
+  bool keep_all = false;
+  if (ckpt_every <= 0) {
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    keep_all = (double)(steps + 2 + c + 2) * (double)sb <= 0.75 * (double)free_b;
+  }
+  bfe_stats& stt = pl->last;
+  stt = bfe_stats{};
+  stt.n_dof = n;
+  stt.nnz_stored = pl->nnz_operator;
+  stt.nnz_padded = pl->nnz_padded;
+  stt.n_interface = pl->n_int;
+  stt.n_direct_rows = pl->n_direct_rows;
+  stt.n_nodes = pl->n_nodes;
+  stt.n_groups = pl->have_groups ? pl->groups.n_groups : 0;
+  stt.variant = variant;
+  stt.adjoint_segments = n_seg;
+  stt.adjoint_kept = keep_all ? 1 : 0;
+  stt.step_launches = (keep_all ? 2 : 3) * steps;
+  DevBuf<unsigned char> d_u, d_ck, d_all;
+  if (keep_all) {
+    CUDA_TRY(d_all.alloc((size_t)(steps + 2) * sb));
+    CUDA_TRY(cudaMemsetAsync(d_all.p, 0, 2 * sb, st));
+    for (int64_t t = ti0; t < n_t; ++t) {
+      af.ti = t;
+      af.u_prev = d_all.p + (size_t)(t - ti0) * sb;
+      af.u_n = d_all.p + (size_t)(t - ti0 + 1) * sb;
+      af.u_new = d_all.p + (size_t)(t - ti0 + 2) * sb;
+      if ((rc = step(af))) return rc;
+    }
+  } else {
+    CUDA_TRY(d_u.alloc(3 * sb));
+    CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * sb, st));
+    CUDA_TRY(d_ck.alloc(2 * sb * n_seg));
+    unsigned char* U[3] = {d_u.p, d_u.p + sb, d_u.p + 2 * sb};
+    int ip = 0, ic = 1, iw = 2;
+    for (int64_t t = ti0; t < n_t; ++t) {
+      if ((t - ti0) % c == 0) {
+        const int64_t j = (t - ti0) / c;
+        CUDA_TRY(cudaMemcpyAsync(d_ck.p + 2 * sb * j, U[ip], sb, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_ck.p + 2 * sb * j + sb, U[ic], sb, cudaMemcpyDeviceToDevice, st));
+      }
+      af.ti = t;
+      af.u_prev = U[ip];
+      af.u_n = U[ic];
+      af.u_new = U[iw];
+      if ((rc = step(af))) return rc;
+      const int tt = ip; ip = ic; ic = iw; iw = tt;
+    }
+  }
+  // element data on the device, prepared on the host while the forward
+  // march runs (the plan's stream does not wait for the legacy stream)
   DevBuf<int32_t> d_dof;
   DevBuf<unsigned char> d_ke, d_mh, d_ch;
   {
     std::vector<int32_t> hd(el_dof, el_dof + n_el * ndf);
     CUDA_TRY(d_dof.upload(hd));
-    CUDA_TRY(d_ke.upload(cast_bytes(prec, ke, n_el * ndf * ndf)));
     CUDA_TRY(d_mh.upload(cast_bytes(prec, mh, n_el * ndf)));
     CUDA_TRY(d_ch.upload(cast_bytes(prec, ch, n_el * ndf)));
   }
@@ -172,66 +269,7 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
       factored = true;
     }
   }
-  // forward inputs
-  const int64_t n_sig = frc_rows * R;
-  DevBuf<double> d_sig, d_hist;
-  {
-    std::vector<double> h((size_t)n_t * n_sig);
-    for (int64_t r = 0; r < R; ++r)
-      for (int64_t ti = 0; ti < n_t; ++ti)
-        for (int64_t k = 0; k < frc_rows; ++k)
-          h[(size_t)ti * n_sig + k + frc_rows * r] = frcs[k + frc_rows * (ti + n_t * r)];
-    CUDA_TRY(d_sig.upload(h));
-  }
-  const size_t hist_n = (size_t)q * n_t * R;
-  CUDA_TRY(d_hist.alloc(hist_n));
-  CUDA_TRY(cudaMemsetAsync(d_hist.p, 0, hist_n * sizeof(double), st));
-  std::vector<int64_t> hidx(hist_idx, hist_idx + q);
-  RunArrays rf;
-  bfe::StepArgs af;
-  if ((rc = prepare_run(pl, frc, hidx, R, n_t, n_sig, d_sig.p, d_hist.p, st, rf, af))) return rc;
-  const bool use_groups = pl->have_groups && (prec == BFE_PREC_SINGLE ? (R % 64 == 0 || R == 16 || R == 32)
-                                                                       : R % 16 == 0);
-  const bfe::GroupArgs* grp = use_groups ? &pl->groups : nullptr;
-  // the variant the forward runs chose for this R, else the default candidate
-  int variant = 0;
-  if (R > 1) {
-    int cand[8];
-    bfe::batched_candidates(prec, (int)R, use_groups, grp ? bfe::group_max_bs(*grp) : 0, cand);
-    variant = cand[0];
-    auto it = pl->variant_of_R.find(R);
-    if (it != pl->variant_of_R.end()) variant = it->second;
-  }
-  auto step = [&](bfe::StepArgs& a) -> int {
-    cudaError_t e = R == 1 ? bfe::launch_step(a, prec, st)
-                           : bfe::launch_step_batched(a, grp, prec, pl->max_slice_entries, variant, st);
-    if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(e));
-    if (pl->n_int) {
-      e = bfe::launch_interface_fixup(a, prec, st);
-      if (e != cudaSuccess) return fail(BFE_ERR_CUDA, "interface kernel launch failed: %s", cudaGetErrorString(e));
-    }
-    return BFE_OK;
-  };
-  const size_t sb = (size_t)n * R * es;
-  DevBuf<unsigned char> d_u, d_ck;
-  CUDA_TRY(d_u.alloc(3 * sb));
-  CUDA_TRY(cudaMemsetAsync(d_u.p, 0, 3 * sb, st));
-  CUDA_TRY(d_ck.alloc(2 * sb * n_seg));
-  unsigned char* U[3] = {d_u.p, d_u.p + sb, d_u.p + 2 * sb};
-  int ip = 0, ic = 1, iw = 2;
-  for (int64_t t = ti0; t < n_t; ++t) {
-    if ((t - ti0) % c == 0) {
-      const int64_t j = (t - ti0) / c;
-      CUDA_TRY(cudaMemcpyAsync(d_ck.p + 2 * sb * j, U[ip], sb, cudaMemcpyDeviceToDevice, st));
-      CUDA_TRY(cudaMemcpyAsync(d_ck.p + 2 * sb * j + sb, U[ic], sb, cudaMemcpyDeviceToDevice, st));
-    }
-    af.ti = t;
-    af.u_prev = U[ip];
-    af.u_n = U[ic];
-    af.u_new = U[iw];
-    if ((rc = step(af))) return rc;
-    const int tt = ip; ip = ic; ic = iw; iw = tt;
-  }
+  if (!factored) CUDA_TRY(d_ke.upload(cast_bytes(prec, ke, n_el * ndf * ndf)));
   // residuals and misfit (FP64, host)
   std::vector<double> hist(hist_n);
   CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -265,7 +303,7 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   // adjoint states lam_t .. lam_{te+1} sit in slots t - ts of d_seg / d_lam
   DevBuf<unsigned char> d_seg, d_lam;
   DevBuf<double> d_gs, d_gr;
-  CUDA_TRY(d_seg.alloc((size_t)(c + 2) * sb));
+  if (!keep_all) CUDA_TRY(d_seg.alloc((size_t)(c + 2) * sb));
   CUDA_TRY(d_lam.alloc((size_t)(c + 2) * sb));
   CUDA_TRY(cudaMemsetAsync(d_lam.p, 0, (size_t)(c + 2) * sb, st));
   CUDA_TRY(d_gs.alloc(n_el));
@@ -304,13 +342,17 @@ int bfe_adjoint_gradient(bfe_plan* pl, int64_t n_el, int32_t ndf, const int64_t*
   }
   for (int64_t j = n_seg - 1; j >= 0; --j) {
     const int64_t ts = ti0 + j * c, te = std::min(ts + c, n_t);
-    CUDA_TRY(cudaMemcpyAsync(S(0), d_ck.p + 2 * sb * j, 2 * sb, cudaMemcpyDeviceToDevice, st));
-    for (int64_t t = ts; t < te; ++t) {
-      af.ti = t;
-      af.u_prev = S(t - ts);
-      af.u_n = S(t - ts + 1);
-      af.u_new = S(t - ts + 2);
-      if ((rc = step(af))) return rc;
+    if (keep_all) {
+      g.u = d_all.p + (size_t)(ts - ti0) * sb;        // slot k: u_{ts + k - 2}
+    } else {
+      CUDA_TRY(cudaMemcpyAsync(S(0), d_ck.p + 2 * sb * j, 2 * sb, cudaMemcpyDeviceToDevice, st));
+      for (int64_t t = ts; t < te; ++t) {
+        af.ti = t;
+        af.u_prev = S(t - ts);
+        af.u_n = S(t - ts + 1);
+        af.u_new = S(t - ts + 2);
+        if ((rc = step(af))) return rc;
+      }
     }
     for (int64_t t = te - 1; t >= ts; --t) {
       aa.ti = t;

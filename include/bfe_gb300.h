@@ -374,12 +374,15 @@ int bfe_run_device(bfe_plan* plan, int64_t R, int64_t n_t, int64_t ti_start,
  *   ke      n_el x ndf x ndf element stiffness at unit scale (with the
  *           absorbing grading of fn_build_global_matrices_v5.m:116)
  *   mh, ch  n_el x ndf element lumped mass and damping per unit density
- * The forward march stores (u_{t-2}, u_{t-1}) every ckpt_every steps
- * (0 = ceil(sqrt(steps))), the backward sweep recomputes each segment from
- * its checkpoint, steps the adjoint through it and contracts the segment
- * into the gradients in one pass. Device memory: about 2 n R (steps / c
- * + c) state values for c = ckpt_every (checkpoints, and the segment's
- * forward and adjoint states). Only 'vel at curent time step' plans with a
+ * The backward sweep runs in segments of c = ckpt_every steps (0 = ceil(
+ * sqrt(steps))): it steps the adjoint through a segment and contracts the
+ * segment into the gradients in one pass. With ckpt_every = 0 the forward
+ * march keeps every state on the device when (steps + c + 4) n R state
+ * values fit in 3/4 of the free device memory, and the sweep contracts
+ * straight from them. Otherwise (or with ckpt_every > 0) it stores
+ * (u_{t-2}, u_{t-1}) every c steps and recomputes each segment from its
+ * checkpoint: about 2 n R (steps / c + c) state values of device memory.
+ * Both give the same gradient. Only 'vel at curent time step' plans with a
  * diagonal P: a plan with fluid-solid interface rows (off-diagonal C from
  * ASI2D2 elements) returns BFE_ERR_UNSUPPORTED.
  * For solid elements (CPE3, bricks) M and C scale with the density, so
@@ -412,6 +415,9 @@ typedef struct bfe_stats {
   int64_t variant;           /* batched kernel variant chosen by the autotuner */
   int64_t n_nodes;           /* nodes given by dof_node / dof_type (0 = no node information) */
   int64_t n_groups;          /* DOF-type groups of the group block-sparse operator (0 = none) */
+  int64_t adjoint_segments;  /* last run an adjoint gradient: its backward segments, else 0 */
+  int64_t adjoint_kept;      /* 1: that adjoint kept every forward state on the device; 0: it
+                                recomputed each segment from a checkpoint */
 } bfe_stats;
 
 /* Enable (1) or disable (0) CUDA-event timing of every launch in later runs. */
