@@ -44,7 +44,7 @@ def build(verbose=False, force=False):
     os.makedirs(OBJ_DIR, exist_ok=True)
     nvcc = _nvcc()
     srcs = _sources()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     objs = []
     jobs = []
