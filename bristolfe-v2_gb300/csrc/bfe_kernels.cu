@@ -216,6 +216,42 @@ __global__ void __launch_bounds__(256) interface_fixup(StepArgs a) {
   if (__ldg(a.rowinfo + row) & kRowMonitored) write_history(a, row, c, (double)r);
 }
 
+// Interface correction with VEC consecutive right-hand sides per thread (R
+// a multiple of VEC): each Z entry and column index is loaded once for VEC
+// values. The sums are interface_fixup's, term for term in the same order.
+template <typename T, typename V, int VEC>
+__global__ void __launch_bounds__(256) interface_fixup_vec(StepArgs a) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int RV = a.R / VEC;
+  if (g >= (int64_t)a.n_int * RV) return;
+  const int t = (int)(g / RV), c = (int)(g % RV) * VEC;
+  const int row = __ldg(a.int_row + t);
+  const T* z = static_cast<const T*>(a.z_val);
+  const T* v = static_cast<const T*>(a.v_int);
+  T acc[VEC];
+#pragma unroll
+  for (int j = 0; j < VEC; ++j) acc[j] = T(0);
+  for (int e = __ldg(a.z_ptr + t); e < __ldg(a.z_ptr + t + 1); ++e) {
+    const T zv = __ldg(z + e);
+    const V x = *reinterpret_cast<const V*>(v + (size_t)__ldg(a.z_col + e) * a.R + c);
+    const T* xs = reinterpret_cast<const T*>(&x);
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) acc[j] = fma(zv, xs[j], acc[j]);
+  }
+  const size_t o = (size_t)row * a.R + c;
+  T* unew = static_cast<T*>(a.u_new);
+  const V bv = a.int_base_prev ? *reinterpret_cast<const V*>(static_cast<const T*>(a.u_prev) + o)
+                               : *reinterpret_cast<const V*>(unew + o);
+  const T* bs = reinterpret_cast<const T*>(&bv);
+  V rv;
+  T* rs = reinterpret_cast<T*>(&rv);
+#pragma unroll
+  for (int j = 0; j < VEC; ++j) rs[j] = bs[j] + acc[j];
+  *reinterpret_cast<V*>(unew + o) = rv;
+  if (__ldg(a.rowinfo + row) & kRowMonitored)
+    for (int j = 0; j < VEC; ++j) write_history(a, row, c + j, (double)rs[j]);
+}
+
 // Interface correction for one right-hand side: one warp per interface row,
 // lanes stride over the row of Z and reduce with shuffles.
 template <typename T>
@@ -418,6 +454,16 @@ cudaError_t launch_interface_fixup(const StepArgs& a, int precision, cudaStream_
     const int blocks = (int)(((int64_t)a.n_int * 32 + threads - 1) / threads);
     if (precision == 0) interface_fixup_r1<double><<<blocks, threads, 0, st>>>(a);
     else interface_fixup_r1<float><<<blocks, threads, 0, st>>>(a);
+    return cudaGetLastError();
+  }
+  if (precision != 0 && a.R % 4 == 0) {
+    const int64_t total = (int64_t)a.n_int * (a.R / 4);
+    interface_fixup_vec<float, float4, 4><<<(int)((total + threads - 1) / threads), threads, 0, st>>>(a);
+    return cudaGetLastError();
+  }
+  if (precision == 0 && a.R % 2 == 0) {
+    const int64_t total = (int64_t)a.n_int * (a.R / 2);
+    interface_fixup_vec<double, double2, 2><<<(int)((total + threads - 1) / threads), threads, 0, st>>>(a);
     return cudaGetLastError();
   }
   const int64_t total = (int64_t)a.n_int * a.R;
