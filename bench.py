@@ -177,11 +177,32 @@ def algorithmic_bytes(nnz, n, R, p, q, b):
     return nnz * (b + 4) + 4 * (n + 1) + 2 * n * b + 3 * R * n * b + R * (p + q) * b
 
 
+SUB_MONITORS = 16      # monitored nodes per steel sub-domain model
+
+
+def workload_config(w, n_sub, n_t, steps_per_march, n_dof, nnz, n_models, n_mon, world, scale):
+    """The `config` object of both arms' JSON lines: the workload itself
+    (the same dict from `--impl ours` and `--impl reference` at a given N);
+    how an arm ran it is reported outside `config`."""
+    R = w["n_src"]
+    return {"workload": "batched multi-source and multi-model: coupled water/steel "
+                        "60x30 mm at 0.05 mm (1.44M triangles, ASI2D2 interface, quadratic "
+                        "absorbers, void blob) with a %d-element array, plus %d steel "
+                        "scatterer sub-domain models of 50k-400k DOF (absorbers, void), "
+                        "%d sources as %d RHS, %d samples" % (R, n_sub, R, R, n_t),
+            "n_dof": int(n_dof), "nnz_K": int(nnz), "models": int(n_models), "sources": R,
+            "monitors": int(n_mon), "samples": int(n_t), "steps_marched_per_source": int(steps_per_march),
+            "l2": "inputs larger than L2 (FP32 state %.0f MB per time step)" % (3 * R * n_dof * 4 / 1e6),
+            "parallelism": ("one GPU" if world == 1 else
+                            "%d ranks, models split by cost, no data-path collective" % world),
+            "scale": scale}
+
+
 def _build_subdomain(args):
     """Worker: one steel sub-domain model (runs in a spawned process)."""
     import bfe_gb300.model as model
     side, seed = args
-    m = model.steel_subdomain(side, seed=seed, n_mon=16)
+    m = model.steel_subdomain(side, seed=seed, n_mon=SUB_MONITORS)
     return {k: m[k] for k in ("K", "C", "M", "gl", "dt", "src_nodes", "mon_nodes")}
 
 
@@ -394,20 +415,12 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched multi-source and multi-model: coupled water/steel "
-                                   "60x30 mm at 0.05 mm (1.44M triangles, ASI2D2 interface, quadratic "
-                                   "absorbers, void blob) with a %d-element array, plus %d steel "
-                                   "scatterer sub-domain models of 50k-400k DOF (absorbers, void), "
-                                   "%d sources as %d RHS, %d samples, FP32 batched, CUDA graph"
-                                   % (R_all, n_sub, R_all, R_all, n_t),
-                       "n_dof": n_all, "nnz_K": int(sum(m["K"].nnz for m in models)), "models": len(models),
-                       "sources": R_all, "monitors": int(sum(len(m["mon_nodes"]) for m in models)),
-                       "samples": n_t, "steps_marched_per_source": steps_per_march,
-                       "l2": "inputs larger than L2 (state %.0f MB per time step on rank 0)" % (3 * R * n * 4 / 1e6),
-                       "parallelism": ("one GPU" if world == 1 else
-                                       "%d ranks, models split by cost, no data-path collective" % world),
-                       "rank0_share": {"models": len(mine), "n_dof": n, "sources": [s_lo, s_hi]},
-                       "scale": args.scale},
+            "config": workload_config(w, n_sub, n_t, steps_per_march, n_all,
+                                      sum(m["K"].count_nonzero() for m in models), len(models),
+                                      sum(len(m["mon_nodes"]) for m in models), world, args.scale),
+            "run": {"kernel_path": "FP32 batched, CUDA graph",
+                    "rank0_share": {"models": len(mine), "n_dof": n, "sources": [s_lo, s_hi],
+                                    "state_mb_per_step": 3 * R * n * 4 / 1e6}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profiled_traffic(kname, n),
                          "kernel": kname, "variant": stk["variant"], "bytes_per_launch": bytes_step,
@@ -875,6 +888,8 @@ def run_reference(args):
     runtime_probe = {k: shutil.which(k) for k in ("matlab", "octave", "octave-cli")}
     from oracle import assembly, cpu_port, mesh, signals
     w = workload(args.scale)
+    if args.sources:
+        w["n_src"] = args.sources
     n_t = args.n_t or w["n_t"]
     steel = dict(rho=8000.0, D=signals.isotropic_stiffness_matrix(210e9, 0.3), el_typ="CPE3")
     water = dict(rho=1000.0, D=1500.0 ** 2 * 1000.0, el_typ="AC2D3")
@@ -940,10 +955,12 @@ def run_reference(args):
         "n_gpus": int(os.environ.get("WORLD_SIZE", 1)), "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "coupled water/steel 60x30 mm at 0.05 mm plus %d steel scatterer "
-                               "sub-domain models joined in one operator, reference CPU v6 loop (FP64), "
-                               "one source per bounded sample" % (n_models - 1),
-                   "n_dof": n, "models": n_models, "samples": n_t, "sample_steps": steps, "scale": args.scale},
+        "config": workload_config(w, n_models - 1, n_t, n_t - int(np.nonzero(sig)[0].min()), n,
+                                  K.count_nonzero(), n_models, w["n_src"] + (n_models - 1) * SUB_MONITORS,
+                                  int(os.environ.get("WORLD_SIZE", 1)), args.scale),
+        "run": {"kernel_path": "reference CPU v6 loop (FP64, the oracle's C port), the models joined in one "
+                               "operator, one source per bounded sample",
+                "sample_steps": steps},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_port.threads(), "kind": "port",
                          "sample": "first %d of %d samples of one source" % (steps, n_t)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
