@@ -178,6 +178,7 @@ def algorithmic_bytes(nnz, n, R, p, q, b):
 
 
 SUB_MONITORS = 16      # monitored nodes per steel sub-domain model
+L2_BYTES = 126 * 2 ** 20   # GB300 L2
 
 
 def workload_config(w, n_sub, n_t, steps_per_march, n_dof, nnz, n_models, n_mon, world, scale):
@@ -192,7 +193,8 @@ def workload_config(w, n_sub, n_t, steps_per_march, n_dof, nnz, n_models, n_mon,
                         "%d sources as %d RHS, %d samples" % (R, n_sub, R, R, n_t),
             "n_dof": int(n_dof), "nnz_K": int(nnz), "models": int(n_models), "sources": R,
             "monitors": int(n_mon), "samples": int(n_t), "steps_marched_per_source": int(steps_per_march),
-            "l2": "inputs larger than L2 (FP32 state %.0f MB per time step)" % (3 * R * n_dof * 4 / 1e6),
+            "l2": ("inputs larger than L2" if 3 * R * n_dof * 4 > L2_BYTES else "inputs within L2") +
+                  " (FP32 state %.0f MB per time step)" % (3 * R * n_dof * 4 / 1e6),
             "parallelism": ("one GPU" if world == 1 else
                             "%d ranks, models split by cost, no data-path collective" % world),
             "scale": scale}
