@@ -26,13 +26,31 @@ __device__ __forceinline__ float4 f4fma(float2 c, float4 x, float4 acc) {   // c
   return make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
+// L1 policies of the state loads: a neighbour row is read again by the
+// node's other neighbours on this SM, so it is kept in L1 (evict_last);
+// u_{n-1} is read once, by its own node, so it does not take L1 space
+// (no_allocate). Measured on the 33-model, 64-source march: 1.073 ms per
+// step against 1.083 with the default policies.
+__device__ __forceinline__ float4 ld_keep(const float* p) {
+  float4 r;
+  asm("ld.global.nc.L1::evict_last.v4.f32 {%0,%1,%2,%3}, [%4];"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float4 ld_once(const float* p) {
+  float4 r;
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+  return r;
+}
+
 // One neighbour block of a node: acc_k += sum_l c_kl (u_own_l - u_nbr_l).
 template <int BS>
 __device__ __forceinline__ void group4_nbr(const float* nb, const float* craw, int e, size_t rs,
                                            const float4 (&uo)[BS], float4 (&acc)[BS]) {
   float4 g[BS];
 #pragma unroll
-  for (int l = 0; l < BS; ++l) g[l] = __ldg(reinterpret_cast<const float4*>(nb + l * rs));
+  for (int l = 0; l < BS; ++l) g[l] = ld_keep(nb + l * rs);
   float2 cv[BS * BS];
   if (BS == 2) {
     const float4 cr = __ldg(reinterpret_cast<const float4*>(craw + (size_t)e * 4));
@@ -136,8 +154,7 @@ __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& 
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
       uo[k] = __ldg(reinterpret_cast<const float4*>(un + (size_t)(row0 + k) * rs + c));
-      up[k] = __ldcs(reinterpret_cast<const float4*>(static_cast<const float*>(a.u_prev) +
-                                                      (size_t)(row0 + k) * rs + c));
+      up[k] = ld_once(static_cast<const float*>(a.u_prev) + (size_t)(row0 + k) * rs + c);
       acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 #pragma unroll (BS == 1 ? 2 : 1)
