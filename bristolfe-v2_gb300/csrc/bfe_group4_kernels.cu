@@ -26,11 +26,11 @@ __device__ __forceinline__ float4 f4fma(float2 c, float4 x, float4 acc) {   // c
   return make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
-// L1 policies of the state loads: a neighbour row is read again by the
-// node's other neighbours on this SM, so it is kept in L1 (evict_last);
-// u_{n-1} is read once, by its own node, so it does not take L1 space
-// (no_allocate). Measured on the 33-model, 64-source march: 1.073 ms per
-// step against 1.083 with the default policies.
+// L1 policies of the state loads: a node's own rows and its neighbour rows
+// are read again by other nodes of the SM, so they are kept in L1
+// (evict_last); u_{n-1} is read once, by its own node, so it does not take
+// L1 space (no_allocate). Measured on the 33-model, 64-source march: 1.065
+// ms per step against 1.083 with the default policies.
 __device__ __forceinline__ float4 ld_keep(const float* p) {
   float4 r;
   asm("ld.global.nc.L1::evict_last.v4.f32 {%0,%1,%2,%3}, [%4];"
@@ -153,7 +153,7 @@ __device__ __forceinline__ void group4_node(const StepArgs& a, const GroupArgs& 
     float4 uo[BS], up[BS], acc[BS];
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
-      uo[k] = __ldg(reinterpret_cast<const float4*>(un + (size_t)(row0 + k) * rs + c));
+      uo[k] = ld_keep(un + (size_t)(row0 + k) * rs + c);
       up[k] = ld_once(static_cast<const float*>(a.u_prev) + (size_t)(row0 + k) * rs + c);
       acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
