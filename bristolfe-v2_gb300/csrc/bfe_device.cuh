@@ -1,5 +1,5 @@
 // Device helpers shared by the step kernels (bfe_kernels.cu,
-// bfe_group_kernels.cu, bfe_tma.cu): forcing and monitor lookups on the
+// bfe_group_kernels.cu, bfe_group4_kernels.cu): forcing and monitor lookups on the
 // sorted per-run lists, and the error-free sums of the compensated update.
 #pragma once
 #include <cuda_runtime.h>

@@ -55,3 +55,20 @@ def test_reference_arm_config_equals_the_product_workload():
                                  sum(m["K"].count_nonzero() for m in models), len(models),
                                  sum(len(m["mon_nodes"]) for m in models), 1, scale)
     assert ref == ours
+
+
+def test_roofline_traffic_record():
+    """The step kernel's DRAM traffic that bench.py reports comes from the
+    committed capture of the full workload: at its own size it is the
+    captured bytes, the other occupancy variant maps to the same record, and
+    an unknown kernel reports none."""
+    sys.path.insert(0, ROOT)
+    import bench
+    with open(os.path.join(ROOT, "profiles", "step_kernel_traffic.json")) as f:
+        rec = json.load(f)["step_f32_group4<12>"]
+    assert bench.profiled_traffic("step_f32_group4<12>", rec["n_dof"]) == rec["dram_bytes_per_launch"]
+    assert bench.profiled_traffic("step_f32_group4<10>", rec["n_dof"]) == rec["dram_bytes_per_launch"]
+    assert bench.profiled_traffic("no such kernel", 1000) is None
+    # the capture's bytes are within 10 % of the algorithmic bytes of that launch
+    alg = bench.algorithmic_bytes(72066387, rec["n_dof"], rec["R"], 9, 576, 4)
+    assert 0.9 < rec["dram_bytes_per_launch"] / alg < 1.1
