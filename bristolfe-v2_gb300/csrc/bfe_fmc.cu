@@ -54,15 +54,16 @@ __global__ void convolve_kernel(int64_t n_t, int64_t n_sig, const double* __rest
                                 const double* __restrict__ g, int64_t g0, int64_t g1,
                                 double* __restrict__ h) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t s = blockIdx.y;
-  if (t >= n_t || s >= n_sig) return;
-  const double* fs = f + s * n_t;
-  double acc = 0.0;
-  const int64_t hi = t < g1 - 1 ? t : g1 - 1;
-  for (int64_t tau = g0; tau <= hi; ++tau) acc = fma(__ldg(g + tau), __ldg(fs + t - tau), acc);
-  for (int64_t tau = (n_t + t + 1 > g0 ? n_t + t + 1 : g0); tau < g1; ++tau)
-    acc = fma(__ldg(g + tau), __ldg(fs + 2 * n_t + t - tau), acc);
-  h[s * n_t + t] = acc;
+  if (t >= n_t) return;
+  for (int64_t s = blockIdx.y; s < n_sig; s += gridDim.y) {
+    const double* fs = f + s * n_t;
+    double acc = 0.0;
+    const int64_t hi = t < g1 - 1 ? t : g1 - 1;
+    for (int64_t tau = g0; tau <= hi; ++tau) acc = fma(__ldg(g + tau), __ldg(fs + t - tau), acc);
+    for (int64_t tau = (n_t + t + 1 > g0 ? n_t + t + 1 : g0); tau < g1; ++tau)
+      acc = fma(__ldg(g + tau), __ldg(fs + 2 * n_t + t - tau), acc);
+    h[s * n_t + t] = acc;
+  }
 }
 
 // time_data[t, k] = sum_e w_e hist[slot_e, t, tx_k] over receiver k's entries.
@@ -71,12 +72,13 @@ __global__ void fmc_gather_kernel(int64_t q, int64_t n_t, const double* __restri
                                   const int32_t* __restrict__ slot, const double* __restrict__ w,
                                   double* __restrict__ out) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t k = blockIdx.y;
-  if (t >= n_t || k >= n_pairs) return;
-  const double* hb = hist + (size_t)q * ((size_t)t + (size_t)n_t * __ldg(pair_tx + k));
-  double acc = 0.0;
-  for (int e = __ldg(ptr + k); e < __ldg(ptr + k + 1); ++e) acc = fma(__ldg(w + e), __ldg(hb + __ldg(slot + e)), acc);
-  out[(size_t)k * n_t + t] = acc;
+  if (t >= n_t) return;
+  for (int64_t k = blockIdx.y; k < n_pairs; k += gridDim.y) {
+    const double* hb = hist + (size_t)q * ((size_t)t + (size_t)n_t * __ldg(pair_tx + k));
+    double acc = 0.0;
+    for (int e = __ldg(ptr + k); e < __ldg(ptr + k + 1); ++e) acc = fma(__ldg(w + e), __ldg(hb + __ldg(slot + e)), acc);
+    out[(size_t)k * n_t + t] = acc;
+  }
 }
 
 // force[fr, t] = m_r accn_r(t) + C(r,:) vel(t) + K(r,:) disp(t) for the force
@@ -89,34 +91,41 @@ __global__ void forces_kernel(int64_t n, int64_t n_t, int64_t n_force, const int
                               const double* __restrict__ d, double dt, int vel_current,
                               double* __restrict__ out) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t fr = blockIdx.y;
-  if (t >= n_t || fr >= n_force) return;
+  if (t >= n_t) return;
   auto disp = [&](int64_t j, int64_t tt) -> double {     // d(j, tt), zero before the first sample
     return (tt < 0 || frozen[j]) ? 0.0 : __ldg(d + j + n * tt);
   };
-  const int r = rows[fr];
-  const double accn = (disp(r, t) - 2 * disp(r, t - 1) + disp(r, t - 2)) / (dt * dt);
-  double acc = m[r] * accn;
-  double sc = 0.0;
-  for (int e = cp[r]; e < cp[r + 1]; ++e) {
-    const int j = cc[e];
-    const double v = vel_current ? (disp(j, t) - disp(j, t - 2)) / (2 * dt) : (disp(j, t - 1) - disp(j, t - 2)) / dt;
-    sc = fma(cv[e], v, sc);
+  for (int64_t fr = blockIdx.y; fr < n_force; fr += gridDim.y) {
+    const int r = rows[fr];
+    const double accn = (disp(r, t) - 2 * disp(r, t - 1) + disp(r, t - 2)) / (dt * dt);
+    double acc = m[r] * accn;
+    double sc = 0.0;
+    for (int e = cp[r]; e < cp[r + 1]; ++e) {
+      const int j = cc[e];
+      const double v = vel_current ? (disp(j, t) - disp(j, t - 2)) / (2 * dt) : (disp(j, t - 1) - disp(j, t - 2)) / dt;
+      sc = fma(cv[e], v, sc);
+    }
+    double sk = 0.0;
+    for (int e = kp[r]; e < kp[r + 1]; ++e) sk = fma(kv[e], disp(kc[e], t - 1), sk);
+    out[(size_t)t * n_force + fr] = acc + sc + sk;
   }
-  double sk = 0.0;
-  for (int e = kp[r]; e < kp[r + 1]; ++e) sk = fma(kv[e], disp(kc[e], t - 1), sk);
-  out[(size_t)t * n_force + fr] = acc + sc + sk;
 }
 
 // F[s][k] *= G[k] * scale for the n_sig spectra of nc bins.
 __global__ void spectrum_product_kernel(int64_t nc, int64_t n_sig, cufftDoubleComplex* __restrict__ F,
                                         const cufftDoubleComplex* __restrict__ G, double scale) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t s = blockIdx.y;
-  if (k >= nc || s >= n_sig) return;
-  const cufftDoubleComplex a = F[s * nc + k], b = G[k];
-  F[s * nc + k] = make_cuDoubleComplex((a.x * b.x - a.y * b.y) * scale, (a.x * b.y + a.y * b.x) * scale);
+  if (k >= nc) return;
+  const cufftDoubleComplex b = G[k];
+  for (int64_t s = blockIdx.y; s < n_sig; s += gridDim.y) {
+    const cufftDoubleComplex a = F[s * nc + k];
+    F[s * nc + k] = make_cuDoubleComplex((a.x * b.x - a.y * b.y) * scale, (a.x * b.y + a.y * b.x) * scale);
+  }
 }
+
+// Blocks along y of the kernels above: one per signal, pair or force row, at
+// most 65,535 (the grid's y limit); the kernels loop over the rest.
+inline unsigned grid_y(int64_t n) { return (unsigned)(n < 65535 ? n : 65535); }
 
 // Supports longer than this many samples take the FFT route.
 constexpr int64_t kFftSupport = 256;
@@ -165,7 +174,7 @@ int launch_convolve_fft(int64_t n_t, int64_t n_sig, const double* d_f, const dou
   CUFFT_TRY(cufftSetStream(inv.h, st));
   CUFFT_TRY(cufftExecD2Z(fwd.h, pad.p, F.p));
   CUFFT_TRY(cufftExecD2Z(one.h, gpad.p, G.p));
-  const dim3 grid((unsigned)((nc + 255) / 256), (unsigned)n_sig);
+  const dim3 grid((unsigned)((nc + 255) / 256), grid_y(n_sig));
   spectrum_product_kernel<<<grid, 256, 0, st>>>(nc, n_sig, F.p, G.p, 1.0 / (double)L);
   FTRY(cudaGetLastError());
   CUFFT_TRY(cufftExecZ2D(inv.h, F.p, pad.p));
@@ -194,7 +203,7 @@ int launch_convolve(int64_t n_t, int64_t n_sig, const double* d_f, const double*
   if (g1 <= g0) {
     FTRY(cudaMemsetAsync(d_h, 0, (size_t)n_t * n_sig * sizeof(double), st));
   } else {
-    const dim3 grid((unsigned)((n_t + 127) / 128), (unsigned)n_sig);
+    const dim3 grid((unsigned)((n_t + 127) / 128), grid_y(n_sig));
     convolve_kernel<<<grid, 128, 0, st>>>(n_t, n_sig, d_f, d_g.p, g0, g1, d_h);
     FTRY(cudaGetLastError());
   }
@@ -264,7 +273,7 @@ int bfe_fmc_gather_device(int64_t q, int64_t n_t, int64_t R, const double* d_his
     FTRY(d_raw.alloc((size_t)n_t * n_pairs));
     gather_out = d_raw.p;
   }
-  const dim3 grid((unsigned)((n_t + 127) / 128), (unsigned)n_pairs);
+  const dim3 grid((unsigned)((n_t + 127) / 128), grid_y(n_pairs));
   fmc_gather_kernel<<<grid, 128, 0, st>>>(q, n_t, d_hist, n_pairs, d_tx.p, d_ptr.p, d_slot.p, d_w.p, gather_out);
   FTRY(cudaGetLastError());
   if (conv) return launch_convolve(n_t, n_pairs, d_raw.p, in_sig, n_g, d_time_data, st);
@@ -371,7 +380,7 @@ int bfe_disps_to_forces(const bfe_sparse* K, const bfe_sparse* C, const bfe_spar
   FTRY(d_fr.upload(frozen.data(), frozen.size(), st));
   FTRY(d_d.upload(disp, (size_t)n * n_t, st));
   FTRY(d_out.alloc(rows.size() * (size_t)n_t));
-  const dim3 grid((unsigned)((n_t + 127) / 128), (unsigned)rows.size());
+  const dim3 grid((unsigned)((n_t + 127) / 128), grid_y((int64_t)rows.size()));
   forces_kernel<<<grid, 128, 0, st>>>(n, n_t, (int64_t)rows.size(), d_rows.p, d_m.p, d_kp.p, d_kc.p, d_kv.p,
                                       d_cp.p, d_cc.p, d_cv.p, d_fr.p, d_d.p, dt,
                                       solver_mode == BFE_MODE_VEL_CURRENT, d_out.p);
